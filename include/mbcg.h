@@ -1,0 +1,193 @@
+/*
+ * mbcg.h -- C ABI of the GB300 moment-based colour-gradient lattice Boltzmann step
+ * (D3Q19 / D3Q27), a drop-in for the reference solver's time-step path.
+ *
+ * Lattice convention (same as the reference, utilities/indexing.cuh:10-14 and
+ * utilities/bounds.cuh:12-20): an NX x NY x NZ box whose outermost layer on every axis is
+ * a ghost frame.  Fluid nodes are 1..N-2 on each axis; the node (x,y,z) of field f lives at
+ * f[x + y*pitch + z*pitch*NY] (pitch = NX in the reference's dense layout).  Periodic axes
+ * wrap over the N-2 fluid nodes (bounds.cuh:34-77).
+ *
+ * State: 11 SoA moment fields per node, in this order (memory.cuh:14-29):
+ *   0 rhor, 1 rhob, 2 ux, 3 uy, 4 uz, 5 Pixx, 6 Pixy, 7 Piyy, 8 Piyz, 9 Pizz, 10 Pixz.
+ * In the FP16/BF16 storage form the same 11 slots hold scaled deviations:
+ *   0 (rho - rho_nominal(phi)) / rho_scale, 1 phi = (rhor-rhob)/rho,
+ *   2..4 u / u_ref, 5..10 Pi / pi_scale.
+ *
+ * Every function returns 0 on success and a negative MBCG_E* code on failure; the text of
+ * the last error of the calling thread is available from mbcg_last_error().  Nothing here
+ * calls exit() (the reference's CUDA_CHECK does, utilities/cudaUtilities.cuh:9-19).
+ * Streams are caller-provided; a case handle must be driven by one host thread at a time.
+ */
+#ifndef MBCG_H
+#define MBCG_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *mbcg_stream_t; /* == cudaStream_t; NULL = legacy default stream */
+
+/* ---- enumerations ------------------------------------------------------------------ */
+#define MBCG_NFIELDS 11
+
+/* per-axis boundary kind */
+#define MBCG_BC_PERIODIC 0 /* wrap over the N-2 fluid nodes (bounds.cuh:34-77)                 */
+#define MBCG_BC_INOUT    1 /* jet axis: inlet ghost at 0, outlet ghost at N-1 (lbm.cuh:79-151,
+                              jet/boundary_conditions.cuh:16-109)                             */
+#define MBCG_BC_WALL     2 /* no-slip walls on the ghost layers 0 and N-1 (halfway bounce-back)*/
+
+/* outlet kind for the INOUT axis */
+#define MBCG_OUTLET_CONVECTIVE   0 /* reference: jet/boundary_conditions.cuh:45-109            */
+#define MBCG_OUTLET_ZERO_GRADIENT 1 /* ghost = copy of the last fluid layer                      */
+
+/* moment storage precision */
+#define MBCG_FP32 0
+#define MBCG_FP16 1
+#define MBCG_BF16 2
+
+/* initial-condition functor */
+#define MBCG_IC_JET    0 /* jet/jetIn.cuh:16-60        */
+#define MBCG_IC_BUBBLE 1 /* bubble/bubbleIn.cuh:15-52  */
+#define MBCG_IC_RTI    2 /* rti/rtiIn.cuh:18-119       */
+#define MBCG_IC_NONE   3 /* leave the state as copied in */
+
+/* error codes */
+#define MBCG_OK            0
+#define MBCG_E_INVALID    -1 /* bad parameter                        */
+#define MBCG_E_CUDA       -2 /* a CUDA runtime / driver call failed    */
+#define MBCG_E_NOMEM      -3 /* device allocation failed               */
+#define MBCG_E_TIMEOUT    -4 /* a bounded device wait gave up           */
+#define MBCG_E_UNSUPPORTED -5
+
+/* ---- case parameters (runtime replacement of the reference's constants.cuh) --------- */
+typedef struct mbcg_params {
+    int32_t q;              /* 19 or 27 (constants.cuh:21-26, stencil_ct.cuh:419-425)     */
+    int32_t nx, ny, nz;     /* lattice size including the ghost frame (constants.cuh:14-16)*/
+    int32_t bc[3];          /* MBCG_BC_* for x, y, z; at most one non-periodic axis        */
+    int32_t outlet;         /* MBCG_OUTLET_*                                               */
+    int32_t precision;      /* MBCG_FP32 / MBCG_FP16 / MBCG_BF16                           */
+    int32_t ic;             /* MBCG_IC_* used by mbcg_init                                 */
+    double tau;             /* relaxation time; oms = 1 - 1/tau (constants.cuh:78-85)       */
+    double sigma;           /* surface tension (constants.cuh:90)                          */
+    double beta;            /* recolouring parameter (constants.cuh:91)                    */
+    double rho_r0, rho_b0;  /* nominal phase densities (constants.cuh:72-73); a ratio != 1
+                               switches on the phase-dependent rest-population equilibrium */
+    double gravity[3];      /* body-force acceleration; force density = rho * g (Guo)      */
+    /* jet case (constants.cuh:31-35, jet/jetIn.cuh, jet/boundary_conditions.cuh) */
+    double jet_radius;
+    double jet_velocity;
+    double jet_center[2];   /* disc centre in the two non-jet axes, in axis order          */
+    double jet_phase;       /* phi of the injected fluid: -1 = blue (reference), +1 = red  */
+    double inlet_noise;     /* relative amplitude of the per-step uniform inlet noise      */
+    uint64_t seed;          /* counter-based RNG seed for the inlet noise                  */
+    /* bubble case (constants.cuh:38-41, bubble/bubbleIn.cuh) */
+    double bubble_radius;
+    double bubble_center[3];
+    double bubble_width;    /* 0 = sharp mask (reference); > 0 = tanh profile width        */
+    double bubble_phase;    /* phi inside the bubble: -1 = blue (reference), +1 = red      */
+    /* Rayleigh-Taylor case (constants.cuh:44-50, rti/rtiIn.cuh); the interface normal is
+       the wall axis (or y when no axis is a wall) */
+    double rti_position;
+    double rti_amplitude;
+    double rti_width;
+    double rti_phase_above; /* phi above the interface: -1 = blue (reference), +1 = red    */
+    int32_t rti_mode[2];    /* modes along the two transverse axes, in axis order          */
+    int32_t reserved0;
+    int32_t reserved1;
+    /* FP16/BF16 storage scales */
+    double rho_scale;       /* (rho - rho_nominal) / rho_scale is stored; default 0.01     */
+    double u_ref;           /* u / u_ref is stored; default 0.05                           */
+    double pi_scale;        /* Pi / pi_scale is stored; default u_ref^2                    */
+} mbcg_params;
+
+/* Fill *p with the reference's shipped constants (constants.cuh:9-93): D3Q27, 128^3 jet
+ * along y, tau = 1, sigma = 0.1, beta = 0.9, jet radius 12, velocity 0.05, blue jet. */
+void mbcg_params_default(mbcg_params *p);
+
+/* ---- moment views ------------------------------------------------------------------ */
+/* 11 device arrays of one state, reference field order; the replacement of the
+ * reference's MomentsDevice (memory.cuh:14-29) with an explicit row pitch. */
+typedef struct mbcg_moments {
+    void *f[MBCG_NFIELDS];
+    int64_t pitch;          /* elements between rows (>= nx)                               */
+    int32_t precision;      /* MBCG_FP32 / MBCG_FP16 / MBCG_BF16                           */
+    int32_t reserved;
+} mbcg_moments;
+
+typedef struct mbcg_diag {
+    double mass_r, mass_b;  /* sum of rhor / rhob over fluid nodes                         */
+    double momentum[3];     /* sum of rho*u over fluid nodes                               */
+    double p_in, p_out;     /* mean pressure inside the bubble core / far field (bubble)   */
+    double dp;              /* p_in - p_out (Laplace pressure jump)                        */
+    int64_t nonfinite;      /* fluid nodes with a non-finite field or rho <= 0             */
+    int64_t nodes;          /* fluid nodes reduced over                                    */
+} mbcg_diag;
+
+/* ---- case handle: library-owned state -------------------------------------------- */
+typedef struct mbcg_case mbcg_case;
+
+/* Validates *p, allocates the two moment states (A current, B next; memory.cuh:153-164)
+ * with a padded row pitch, builds the TMA descriptors.  No kernel runs. */
+int mbcg_create(const mbcg_params *p, mbcg_case **out);
+int mbcg_destroy(mbcg_case *c);
+
+/* Initial condition p->ic on state A, then the initial boundary pass (main.cu:25-26). */
+int mbcg_init(mbcg_case *c, mbcg_stream_t s);
+
+/* nsteps fused steps: RCS (lbm.cuh:20-262) + boundary functors (kernels.cu:102-114) +
+ * swap (memory.cuh:200-203), all in one kernel launch per step. */
+int mbcg_step(mbcg_case *c, int32_t nsteps, mbcg_stream_t s);
+
+/* The reference's split form for drop-in parity: mbcg_rcs writes B from A without the
+ * boundary pass (launch_RCS, launch.cuh:89-94); mbcg_bc applies the boundary functors on B
+ * reading the old state A (launch_JetBoundaryConditions, launch.cuh:78-83); mbcg_swap
+ * exchanges A and B (swap_moments, memory.cuh:200-203). */
+int mbcg_rcs(mbcg_case *c, mbcg_stream_t s);
+int mbcg_bc(mbcg_case *c, mbcg_stream_t s);
+int mbcg_swap(mbcg_case *c);
+
+/* Device views of the current (A) and next (B) states. */
+int mbcg_fields(const mbcg_case *c, mbcg_moments *a, mbcg_moments *b);
+int64_t mbcg_steps_done(const mbcg_case *c);
+
+/* Copies between state A and 11 host FP32 arrays in the reference's dense layout
+ * (pitch = nx, copy_out_D2H in memory.cuh:209-217).  FP16/BF16 states are converted. */
+int mbcg_copy_out(mbcg_case *c, float *const host[MBCG_NFIELDS], mbcg_stream_t s);
+int mbcg_copy_in(mbcg_case *c, const float *const host[MBCG_NFIELDS], mbcg_stream_t s);
+
+/* FP64 on-GPU conservation and Laplace-pressure diagnostics of state A (synchronous). */
+int mbcg_diagnostics(mbcg_case *c, mbcg_diag *out, mbcg_stream_t s);
+
+/* Reads and clears the device status word (non-zero = a bounded wait gave up). */
+int mbcg_status(mbcg_case *c, int32_t *status);
+
+/* ---- raw entry points on caller-owned moment arrays -------------------------------- */
+/* launch_RCS(A, B, cfg) (launch.cuh:89-94) on arrays laid out as in the reference
+ * (any pitch >= nx).  step is the index of the state B will hold (inlet noise key). */
+int mbcg_rcs_moments(const mbcg_params *p, const mbcg_moments *a, const mbcg_moments *b,
+                     int64_t step, mbcg_stream_t s);
+/* launch_JetBoundaryConditions(B, Aold, cfg) (launch.cuh:78-83). */
+int mbcg_bc_moments(const mbcg_params *p, const mbcg_moments *b, const mbcg_moments *a_old,
+                    int64_t step, mbcg_stream_t s);
+/* launch_Init{Jet,StaticBubble,RTI}(A, cfg) (launch.cuh:14-72) for p->ic, followed by the
+ * initial boundary pass for the jet (main.cu:25-26). */
+int mbcg_init_moments(const mbcg_params *p, const mbcg_moments *a, mbcg_stream_t s);
+
+/* Active (fluid) node count used by the MLUPS definition, (nx-2)(ny-2)(nz-2)
+ * (utilities/mlups_count.cuh:24-29). */
+int64_t mbcg_active_nodes(const mbcg_params *p);
+
+/* Number of kernel launches one mbcg_step(c, 1, s) issues. */
+int32_t mbcg_launches_per_step(const mbcg_case *c);
+
+const char *mbcg_last_error(void);
+const char *mbcg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MBCG_H */

@@ -1,0 +1,396 @@
+"""Python face of the mbcg C ABI (include/mbcg.h): parameter presets and a ctypes binding.
+
+The solver itself is the CUDA library ``libmbcg.so`` built next to this file from ``csrc/``;
+every call below goes through its ``extern "C"`` entry points.  There is no CPU fallback:
+``Library()`` raises if the shared object is missing or fails to load.
+
+Case presets follow the reference's cases (``jet/``, ``bubble/``, ``rti/``) and the
+workloads the solver is benchmarked on; sizes are lattice sizes including the one-node ghost
+frame of the reference's layout (``utilities/indexing.cuh:10-14``), so a box of
+``L`` fluid nodes per axis is ``L + 2`` nodes.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmbcg.so")
+
+NFIELDS = 11
+FIELD_NAMES = ("rhor", "rhob", "ux", "uy", "uz", "Pixx", "Pixy", "Piyy", "Piyz", "Pizz", "Pixz")
+
+BC_PERIODIC, BC_INOUT, BC_WALL = 0, 1, 2
+OUTLET_CONVECTIVE, OUTLET_ZERO_GRADIENT = 0, 1
+FP32, FP16, BF16 = 0, 1, 2
+IC_JET, IC_BUBBLE, IC_RTI, IC_NONE = 0, 1, 2, 3
+
+
+class Params(ctypes.Structure):
+    """Mirror of ``mbcg_params`` (include/mbcg.h)."""
+
+    _fields_ = [
+        ("q", ctypes.c_int32),
+        ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+        ("bc", ctypes.c_int32 * 3),
+        ("outlet", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("ic", ctypes.c_int32),
+        ("tau", ctypes.c_double),
+        ("sigma", ctypes.c_double),
+        ("beta", ctypes.c_double),
+        ("rho_r0", ctypes.c_double), ("rho_b0", ctypes.c_double),
+        ("gravity", ctypes.c_double * 3),
+        ("jet_radius", ctypes.c_double),
+        ("jet_velocity", ctypes.c_double),
+        ("jet_center", ctypes.c_double * 2),
+        ("jet_phase", ctypes.c_double),
+        ("inlet_noise", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+        ("bubble_radius", ctypes.c_double),
+        ("bubble_center", ctypes.c_double * 3),
+        ("bubble_width", ctypes.c_double),
+        ("bubble_phase", ctypes.c_double),
+        ("rti_position", ctypes.c_double),
+        ("rti_amplitude", ctypes.c_double),
+        ("rti_width", ctypes.c_double),
+        ("rti_phase_above", ctypes.c_double),
+        ("rti_mode", ctypes.c_int32 * 2),
+        ("reserved0", ctypes.c_int32),
+        ("reserved1", ctypes.c_int32),
+        ("rho_scale", ctypes.c_double),
+        ("u_ref", ctypes.c_double),
+        ("pi_scale", ctypes.c_double),
+    ]
+
+    @property
+    def shape(self):
+        """(nz, ny, nx): numpy shape of one field in the dense reference layout."""
+        return (self.nz, self.ny, self.nx)
+
+    def active_nodes(self) -> int:
+        return (self.nx - 2) * (self.ny - 2) * (self.nz - 2)
+
+    def copy(self) -> "Params":
+        p = Params()
+        ctypes.pointer(p)[0] = self
+        return p
+
+    def describe(self) -> dict:
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if hasattr(v, "__len__") else v
+        return d
+
+
+def default_params() -> Params:
+    """The reference's shipped constants (constants.cuh:9-93): D3Q27 128^3 jet along y."""
+    p = Params()
+    p.q = 27
+    p.nx = p.ny = p.nz = 128
+    p.bc[0], p.bc[1], p.bc[2] = BC_PERIODIC, BC_INOUT, BC_PERIODIC
+    p.outlet = OUTLET_CONVECTIVE
+    p.precision = FP32
+    p.ic = IC_JET
+    p.tau = 1.0
+    p.sigma = 0.1
+    p.beta = 0.9
+    p.rho_r0 = p.rho_b0 = 1.0
+    p.jet_radius = 12.0
+    p.jet_velocity = 0.05
+    p.jet_center[0] = (p.nx - 1) / 2.0
+    p.jet_center[1] = (p.nz - 1) / 2.0
+    p.jet_phase = -1.0
+    p.inlet_noise = 0.0
+    p.seed = 12345
+    p.bubble_radius = 30.0
+    p.bubble_center[0] = (p.nx - 1) / 2.0
+    p.bubble_center[1] = (p.ny - 1) / 2.0
+    p.bubble_center[2] = (p.nz - 1) / 2.0
+    p.bubble_width = 0.0
+    p.bubble_phase = -1.0
+    p.rti_position = (p.ny - 1) / 2.0
+    p.rti_amplitude = 4.0
+    p.rti_width = 4.0
+    p.rti_phase_above = -1.0
+    p.rti_mode[0] = p.rti_mode[1] = 1
+    p.rho_scale = 0.01
+    p.u_ref = 0.05
+    p.pi_scale = 0.05 * 0.05
+    return p
+
+
+def reference_jet_params(nx: int, ny: int, nz: int, q: int = 27, tau: float = 1.0, sigma: float = 0.1,
+                         beta: float = 0.9, radius: float = 12.0, velocity: float = 0.05) -> Params:
+    """The reference's own jet case (jet along y, periodic x/z, convective outlet, blue jet)
+    on an nx*ny*nz lattice, with the constants it is compiled with (constants.cuh)."""
+    p = default_params()
+    p.q = q
+    p.nx, p.ny, p.nz = nx, ny, nz
+    p.tau, p.sigma, p.beta = tau, sigma, beta
+    p.jet_radius, p.jet_velocity = radius, velocity
+    p.jet_center[0] = (nx - 1) / 2.0
+    p.jet_center[1] = (nz - 1) / 2.0
+    p.bubble_center[0] = (nx - 1) / 2.0
+    p.bubble_center[1] = (ny - 1) / 2.0
+    p.bubble_center[2] = (nz - 1) / 2.0
+    p.rti_position = (ny - 1) / 2.0
+    return p
+
+
+def bubble_params(L: int = 64, q: int = 19, radius: Optional[float] = None, width: float = 3.0,
+                  tau: float = 0.8, sigma: float = 0.01, beta: float = 0.7, precision: int = FP32) -> Params:
+    """Static-bubble Laplace case: L^3 fluid nodes, fully periodic, phi = +1 (red) inside a
+    sphere of radius L/4 centred in the box, tanh profile of the given width, rho = 1."""
+    p = default_params()
+    p.q = q
+    p.nx = p.ny = p.nz = L + 2
+    p.bc[0] = p.bc[1] = p.bc[2] = BC_PERIODIC
+    p.ic = IC_BUBBLE
+    p.tau, p.sigma, p.beta = tau, sigma, beta
+    p.bubble_radius = L / 4.0 if radius is None else radius
+    # fluid node i sits at lattice index i + 1: the centre of fluid nodes 0..L-1 is L/2 + 0.5
+    c = L / 2.0 + 0.5
+    p.bubble_center[0] = p.bubble_center[1] = p.bubble_center[2] = c
+    p.bubble_width = width
+    p.bubble_phase = 1.0
+    p.precision = precision
+    return p
+
+
+def rti_params(L: int = 128, H: Optional[int] = None, q: int = 27, ratio: float = 3.0, g: float = 1e-5,
+               tau: float = 0.55, sigma: float = 5e-4, beta: float = 0.7, amplitude: Optional[float] = None,
+               precision: int = FP32) -> Params:
+    """Rayleigh-Taylor case: L x L fluid nodes periodic in x/y, walls on the z ghost layers
+    z = 0 and z = H - 1 (H = 4L lattice planes), heavy red phase (phi = +1, density
+    ratio `ratio`) above z = H/2 + A cos(2 pi x / L) cos(2 pi y / L), gravity along -z."""
+    p = default_params()
+    H = 4 * L if H is None else H
+    p.q = q
+    p.nx = p.ny = L + 2
+    p.nz = H
+    p.bc[0] = p.bc[1] = BC_PERIODIC
+    p.bc[2] = BC_WALL
+    p.ic = IC_RTI
+    p.tau, p.sigma, p.beta = tau, sigma, beta
+    p.rho_r0, p.rho_b0 = ratio, 1.0
+    p.gravity[0], p.gravity[1], p.gravity[2] = 0.0, 0.0, -g
+    p.rti_position = H / 2.0
+    p.rti_amplitude = (0.05 * L) if amplitude is None else amplitude
+    p.rti_width = 4.0
+    p.rti_phase_above = 1.0
+    p.rti_mode[0] = p.rti_mode[1] = 1
+    p.precision = precision
+    return p
+
+
+def jet_params(nx: int = 256, ny: int = 256, nz: int = 1024, q: int = 27, diameter: float = 32.0,
+               velocity: float = 0.05, noise: float = 0.01, tau: float = 0.51, sigma: float = 1e-3,
+               beta: float = 0.7, seed: int = 12345, precision: int = FP32) -> Params:
+    """Liquid-jet case: nx x ny fluid nodes periodic in x/y; inlet ghost plane z = 0 with a
+    disc of the given diameter injecting red fluid (phi = +1) at u_z = velocity plus
+    +-noise*velocity uniform per-node noise on all components each step; zero-gradient
+    outflow on the ghost plane z = nz + 1; nz fluid planes."""
+    p = default_params()
+    p.q = q
+    p.nx, p.ny, p.nz = nx + 2, ny + 2, nz + 2
+    p.bc[0] = p.bc[1] = BC_PERIODIC
+    p.bc[2] = BC_INOUT
+    p.outlet = OUTLET_ZERO_GRADIENT
+    p.ic = IC_JET
+    p.tau, p.sigma, p.beta = tau, sigma, beta
+    p.jet_radius = diameter / 2.0
+    p.jet_velocity = velocity
+    p.jet_center[0] = (p.nx - 1) / 2.0
+    p.jet_center[1] = (p.ny - 1) / 2.0
+    p.jet_phase = 1.0
+    p.inlet_noise = noise
+    p.seed = seed
+    p.u_ref = velocity
+    p.pi_scale = velocity * velocity
+    p.precision = precision
+    return p
+
+
+# ----------------------------------------------------------------------------- ctypes ABI
+class Moments(ctypes.Structure):
+    """Mirror of ``mbcg_moments``."""
+    _fields_ = [("f", ctypes.c_void_p * NFIELDS), ("pitch", ctypes.c_int64),
+                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class Diag(ctypes.Structure):
+    """Mirror of ``mbcg_diag``."""
+    _fields_ = [("mass_r", ctypes.c_double), ("mass_b", ctypes.c_double),
+                ("momentum", ctypes.c_double * 3), ("p_in", ctypes.c_double),
+                ("p_out", ctypes.c_double), ("dp", ctypes.c_double),
+                ("nonfinite", ctypes.c_int64), ("nodes", ctypes.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {"mass_r": self.mass_r, "mass_b": self.mass_b, "momentum": list(self.momentum),
+                "p_in": self.p_in, "p_out": self.p_out, "dp": self.dp,
+                "nonfinite": self.nonfinite, "nodes": self.nodes}
+
+
+class MbcgError(RuntimeError):
+    pass
+
+
+_P = ctypes.POINTER
+_VP = ctypes.c_void_p
+
+_PROTOS = {
+    "mbcg_params_default": (None, [_P(Params)]),
+    "mbcg_create": (ctypes.c_int, [_P(Params), _P(_VP)]),
+    "mbcg_destroy": (ctypes.c_int, [_VP]),
+    "mbcg_init": (ctypes.c_int, [_VP, _VP]),
+    "mbcg_step": (ctypes.c_int, [_VP, ctypes.c_int32, _VP]),
+    "mbcg_rcs": (ctypes.c_int, [_VP, _VP]),
+    "mbcg_bc": (ctypes.c_int, [_VP, _VP]),
+    "mbcg_swap": (ctypes.c_int, [_VP]),
+    "mbcg_fields": (ctypes.c_int, [_VP, _P(Moments), _P(Moments)]),
+    "mbcg_steps_done": (ctypes.c_int64, [_VP]),
+    "mbcg_copy_out": (ctypes.c_int, [_VP, _VP * NFIELDS, _VP]),
+    "mbcg_copy_in": (ctypes.c_int, [_VP, _VP * NFIELDS, _VP]),
+    "mbcg_diagnostics": (ctypes.c_int, [_VP, _P(Diag), _VP]),
+    "mbcg_status": (ctypes.c_int, [_VP, _P(ctypes.c_int32)]),
+    "mbcg_rcs_moments": (ctypes.c_int, [_P(Params), _P(Moments), _P(Moments), ctypes.c_int64, _VP]),
+    "mbcg_bc_moments": (ctypes.c_int, [_P(Params), _P(Moments), _P(Moments), ctypes.c_int64, _VP]),
+    "mbcg_init_moments": (ctypes.c_int, [_P(Params), _P(Moments), _VP]),
+    "mbcg_active_nodes": (ctypes.c_int64, [_P(Params)]),
+    "mbcg_launches_per_step": (ctypes.c_int32, [_VP]),
+    "mbcg_last_error": (ctypes.c_char_p, []),
+    "mbcg_version": (ctypes.c_char_p, []),
+}
+
+
+class Library:
+    """ctypes handle on libmbcg.so; raises if the CUDA library is absent."""
+
+    _instance = None
+
+    def __init__(self, path: str = LIB_PATH):
+        if not os.path.exists(path):
+            raise MbcgError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+        self.path = path
+        self.lib = ctypes.CDLL(path)
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(self.lib, name)
+            fn.restype = res
+            fn.argtypes = args
+
+    @classmethod
+    def get(cls) -> "Library":
+        if cls._instance is None:
+            cls._instance = Library()
+        return cls._instance
+
+    def check(self, rc: int, what: str) -> None:
+        if rc != 0:
+            msg = self.lib.mbcg_last_error()
+            raise MbcgError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def __getattr__(self, name):
+        return getattr(self.lib, name)
+
+
+def _stream_ptr(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)  # torch.cuda.Stream
+
+
+class Case:
+    """Library-owned simulation state (mbcg_case*)."""
+
+    def __init__(self, params: Params, lib: Optional[Library] = None):
+        self.lib = lib or Library.get()
+        self.params = params.copy()
+        h = ctypes.c_void_p()
+        self.lib.check(self.lib.mbcg_create(ctypes.byref(self.params), ctypes.byref(h)), "mbcg_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mbcg_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init(self, stream=None):
+        self.lib.check(self.lib.mbcg_init(self.handle, _stream_ptr(stream)), "mbcg_init")
+
+    def step(self, n: int = 1, stream=None):
+        self.lib.check(self.lib.mbcg_step(self.handle, int(n), _stream_ptr(stream)), "mbcg_step")
+
+    def rcs(self, stream=None):
+        self.lib.check(self.lib.mbcg_rcs(self.handle, _stream_ptr(stream)), "mbcg_rcs")
+
+    def bc(self, stream=None):
+        self.lib.check(self.lib.mbcg_bc(self.handle, _stream_ptr(stream)), "mbcg_bc")
+
+    def swap(self):
+        self.lib.check(self.lib.mbcg_swap(self.handle), "mbcg_swap")
+
+    @property
+    def steps_done(self) -> int:
+        return int(self.lib.mbcg_steps_done(self.handle))
+
+    def fields(self):
+        a, b = Moments(), Moments()
+        self.lib.check(self.lib.mbcg_fields(self.handle, ctypes.byref(a), ctypes.byref(b)), "mbcg_fields")
+        return a, b
+
+    def copy_out(self, stream=None, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """State A as an (11, nz, ny, nx) float32 array in the reference's dense layout."""
+        p = self.params
+        if out is None:
+            out = np.empty((NFIELDS,) + p.shape, dtype=np.float32)
+        ptrs = (_VP * NFIELDS)(*[out[f].ctypes.data for f in range(NFIELDS)])
+        self.lib.check(self.lib.mbcg_copy_out(self.handle, ptrs, _stream_ptr(stream)), "mbcg_copy_out")
+        return out
+
+    def copy_in(self, state: np.ndarray, stream=None):
+        state = np.ascontiguousarray(state, dtype=np.float32)
+        ptrs = (_VP * NFIELDS)(*[state[f].ctypes.data for f in range(NFIELDS)])
+        self.lib.check(self.lib.mbcg_copy_in(self.handle, ptrs, _stream_ptr(stream)), "mbcg_copy_in")
+
+    def diagnostics(self, stream=None) -> dict:
+        d = Diag()
+        self.lib.check(self.lib.mbcg_diagnostics(self.handle, ctypes.byref(d), _stream_ptr(stream)),
+                       "mbcg_diagnostics")
+        return d.as_dict()
+
+    def status(self) -> int:
+        s = ctypes.c_int32(0)
+        self.lib.check(self.lib.mbcg_status(self.handle, ctypes.byref(s)), "mbcg_status")
+        return int(s.value)
+
+    def launches_per_step(self) -> int:
+        return int(self.lib.mbcg_launches_per_step(self.handle))
+
+
+def moments_from_tensors(tensors: Sequence, pitch: int, precision: int = FP32) -> Moments:
+    """mbcg_moments view over 11 device tensors (torch) in the reference layout."""
+    m = Moments()
+    for f in range(NFIELDS):
+        m.f[f] = tensors[f].data_ptr()
+    m.pitch = pitch
+    m.precision = precision
+    return m

@@ -1,0 +1,111 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Run where the reference sources are mounted (they are compiled, unmodified, into host
+shared objects by oracle/Makefile `shim`; see oracle/ref_shim.cpp):
+
+    python tests/golden/make_golden.py
+
+Each fixture is an .npz with the case parameters (JSON), the input state and the
+reference's output states, all in the reference's dense layout (11, nz, ny, nx).  The
+fixtures pin both the CPU oracle (tests/test_oracle_golden.py) and the CUDA library
+(tests/test_gpu_parity.py) on machines where the reference is absent.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+import oracle_lib as ol  # noqa: E402
+import mbcg  # noqa: E402
+
+
+def random_mixed_state(p: mbcg.Params, seed: int, dtype) -> np.ndarray:
+    """Seeded state with both colours everywhere (every node is an interface node),
+    non-zero velocity and non-equilibrium moments: exercises every term of the step."""
+    rng = np.random.default_rng(seed)
+    s = np.zeros((11,) + p.shape)
+    s[0] = rng.uniform(0.05, 1.0, p.shape)
+    s[1] = rng.uniform(0.05, 1.0, p.shape)
+    s[2:5] = rng.uniform(-0.05, 0.05, (3,) + p.shape)
+    s[5:11] = rng.uniform(-2e-3, 2e-3, (6,) + p.shape)
+    return s.astype(dtype)
+
+
+def save(name: str, p: mbcg.Params, **arrays):
+    meta = json.dumps(p.describe())
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, params=np.array(meta), **arrays)
+    print("wrote", path, {k: v.shape for k, v in arrays.items()})
+
+
+def jet_fixture(q: int):
+    """Reference jet case (jet along y) from its own initial condition: states at steps
+    1, 10 and 100 of main.cu's loop."""
+    p = mbcg.reference_jet_params(18, 14, 12, q=q, tau=0.8, sigma=0.05, beta=0.7, radius=3.0, velocity=0.05)
+    sh = ol.Shim(f"golden_jet{q}", p, "float")
+    a = sh.init("jet")
+    out = {"init": a.copy()}
+    cur = a.copy()
+    nxt = a.copy()
+    for n in range(1, 101):
+        sh.lib.ref_step(ol._ptrs(cur), ol._ptrs(nxt), 1, 1)
+        cur, nxt = nxt, cur
+        if n in (1, 10, 100):
+            out[f"step{n}"] = cur.copy()
+    save(f"ref_jet_q{q}", p, **out)
+
+
+def defaults_fixture():
+    """The reference exactly as shipped (tau = 1, sigma = 0.1, beta = 0.9, jet radius 12,
+    velocity 0.05, D3Q27) on a 32 x 24 x 32 lattice: 20 steps."""
+    p = mbcg.reference_jet_params(32, 24, 32, q=27, tau=1.0, sigma=0.1, beta=0.9, radius=12.0)
+    sh = ol.Shim("golden_defaults", p, "float")
+    a = sh.init("jet")
+    cur, nxt = a.copy(), a.copy()
+    for _ in range(20):
+        sh.lib.ref_step(ol._ptrs(cur), ol._ptrs(nxt), 1, 1)
+        cur, nxt = nxt, cur
+    save("ref_defaults_q27", p, init=a, step20=cur)
+
+
+def random_fixture(q: int):
+    """One RCS + boundary step from a random mixed state, in FP32 and in FP64."""
+    p = mbcg.reference_jet_params(12, 10, 9, q=q, tau=0.7, sigma=0.05, beta=0.7, radius=3.0)
+    out = {}
+    for real, dt in (("float", np.float32), ("double", np.float64)):
+        sh = ol.Shim(f"golden_rand{q}_{real}", p, real)
+        a = random_mixed_state(p, 1000 + q, dt)
+        out[f"in_{real}"] = a
+        out[f"out_{real}"] = sh.step(a.copy(), 1, 1, b=a.copy())
+        out[f"rcs_{real}"] = sh.step(a.copy(), 1, 0, b=a.copy())
+    save(f"ref_random_q{q}", p, **out)
+
+
+def ic_fixture():
+    """Initial-condition functors of the bubble and RTI cases (bubbleIn.cuh, rtiIn.cuh)."""
+    p = mbcg.reference_jet_params(20, 18, 16, q=27)
+    p.bubble_radius = 5.0
+    p.rti_amplitude = 2.0
+    p.rti_width = 3.0
+    sh = ol.Shim("golden_ic", p, "float")
+    save("ref_ic", p, bubble=sh.init("bubble"), rti=sh.init("rti"))
+
+
+def main():
+    if not ol.reference_available():
+        raise SystemExit("reference sources not found; set MBCG_REF_ROOT")
+    for q in (27, 19):
+        jet_fixture(q)
+        random_fixture(q)
+    defaults_fixture()
+    ic_fixture()
+
+
+if __name__ == "__main__":
+    main()
