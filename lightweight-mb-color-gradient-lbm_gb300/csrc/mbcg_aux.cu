@@ -1,0 +1,477 @@
+// mbcg_aux.cu -- the small kernels around the fused step: the standalone inlet/outlet pass
+// (the reference's split launch_JetBoundaryConditions), the case initial conditions, the
+// FP64 conservation / Laplace diagnostics and the dense-layout conversions used by
+// copy-in / copy-out.  None of these is on the per-step hot path of mbcg_step().
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "mbcg_internal.h"
+
+namespace mbcg {
+
+namespace {
+
+template <typename S>
+__device__ __forceinline__ void load_node(const StepParams& P, const void* const* f, long long o, float (&v)[NF]) {
+#pragma unroll
+    for (int i = 0; i < NF; ++i) v[i] = Codec<S>::to_f(static_cast<const S*>(f[i])[o]);
+}
+
+// stored slots -> reference moments (rhor, rhob, u, Pi)
+template <typename S>
+__device__ __forceinline__ void to_moments(const StepParams& P, float (&v)[NF]) {
+    if constexpr (sizeof(S) != 4) {
+        const float phi = v[1];
+        const float rho = P.rho_mean + phi * P.rho_half_diff + P.rho_scale * v[0];
+        v[0] = 0.5f * rho * (1.0f + phi);
+        v[1] = 0.5f * rho * (1.0f - phi);
+        for (int i = 2; i < 5; ++i) v[i] *= P.u_ref;
+        for (int i = 5; i < NF; ++i) v[i] *= P.pi_scale;
+    }
+}
+
+// reference moments -> stored slots
+template <typename S>
+__device__ __forceinline__ void store_moments(const StepParams& P, void* const* f, long long o, const float (&m)[NF]) {
+    if constexpr (sizeof(S) == 4) {
+#pragma unroll
+        for (int i = 0; i < NF; ++i) static_cast<float*>(f[i])[o] = m[i];
+    } else {
+        const float rho = m[0] + m[1];
+        const float phi = (m[0] - m[1]) / rho;
+        static_cast<S*>(f[0])[o] = Codec<S>::from_f((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale);
+        static_cast<S*>(f[1])[o] = Codec<S>::from_f(phi);
+        for (int i = 2; i < 5; ++i) static_cast<S*>(f[i])[o] = Codec<S>::from_f(m[i] * P.inv_u_ref);
+        for (int i = 5; i < NF; ++i) static_cast<S*>(f[i])[o] = Codec<S>::from_f(m[i] * P.inv_pi_scale);
+    }
+}
+
+__device__ __forceinline__ long long lin(const StepParams& P, int x, int y, int z) {
+    return static_cast<long long>(z) * P.plane + static_cast<long long>(y) * P.pitch + x;
+}
+
+__device__ __forceinline__ void transverse(int a, int& t0, int& t1) {
+    t0 = a == 0 ? 1 : 0;
+    t1 = a == 2 ? 1 : 2;
+}
+
+// isJet (utilities/mathUtilities.cuh:39-45), no fused multiply-adds so the mask matches the
+// reference's float arithmetic exactly
+__device__ __forceinline__ float jet_mask(const StepParams& P, int u, int v) {
+    const float du = __fsub_rn(static_cast<float>(u), P.jet_c0);
+    const float dv = __fsub_rn(static_cast<float>(v), P.jet_c1);
+    return __fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv)) <= __fmul_rn(P.jet_radius, P.jet_radius) ? 1.0f : 0.0f;
+}
+
+// ---------------------------------------------------------------- inlet / outlet functors
+// kernels.cu:102-114 on B with the old state Aold (P.a = Aold, P.b = B); jet/
+// boundary_conditions.cuh:16-109.  noise: apply the per-step inlet perturbation.
+template <typename S>
+__global__ void bc_kernel(const StepParams P, int init_inlet) {
+    const int a = P.inout_axis;
+    int t0, t1;
+    transverse(a, t0, t1);
+    const int n3[3] = {P.nx, P.ny, P.nz};
+    const int n0 = n3[t0] - 2, n1 = n3[t1] - 2;
+    const long long total = static_cast<long long>(n0) * n1;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int u = 1 + static_cast<int>(e % n0), v = 1 + static_cast<int>(e / n0);
+        int pb[3], pf[3];
+        pb[t0] = pf[t0] = u;
+        pb[t1] = pf[t1] = v;
+        // inlet
+        pb[a] = 0;
+        pf[a] = 1;
+        {
+            const long long ob = lin(P, pb[0], pb[1], pb[2]), of = lin(P, pf[0], pf[1], pf[2]);
+            float fv[NF];
+            load_node<S>(P, P.b, of, fv);
+            to_moments<S>(P, fv);
+            const float m = jet_mask(P, u, v);
+            float g[NF];
+            g[0] = P.jet_blue ? (1.0f - m) * P.rho_r0 : m * P.rho_r0;
+            g[1] = P.jet_blue ? m * P.rho_b0 : (1.0f - m) * P.rho_b0;
+            g[2] = g[3] = g[4] = 0.0f;
+            g[2 + a] = m * P.jet_velocity;
+            if (!init_inlet && P.noise_amp != 0.0f && m != 0.0f) {
+                const unsigned long long node = static_cast<unsigned long long>(pb[0]) +
+                                                static_cast<unsigned long long>(pb[1]) * P.nx +
+                                                static_cast<unsigned long long>(pb[2]) * P.nx * P.ny;
+                for (int c = 0; c < 3; ++c) g[2 + c] += m * P.noise_amp * noise_xi(P.seed, P.step, node, c);
+            }
+            for (int i = 5; i < NF; ++i) g[i] = init_inlet ? 0.0f : fv[i];
+            store_moments<S>(P, P.b, ob, g);
+        }
+        if (init_inlet) continue;
+        // outlet
+        pb[a] = n3[a] - 1;
+        pf[a] = n3[a] - 2;
+        {
+            const long long ob = lin(P, pb[0], pb[1], pb[2]), of = lin(P, pf[0], pf[1], pf[2]);
+            float fv[NF];
+            load_node<S>(P, P.b, of, fv);
+            to_moments<S>(P, fv);
+            float g[NF];
+            if (P.outlet == MBCG_OUTLET_ZERO_GRADIENT) {
+                for (int i = 0; i < NF; ++i) g[i] = fv[i];
+            } else {
+                float ov[NF];
+                load_node<S>(P, P.a, ob, ov);
+                to_moments<S>(P, ov);
+                const float uc = fminf(fmaxf(fv[2 + a], 0.0f), 1.0f);
+                if (ov[0] + ov[1] <= 1.0e-20f) {
+                    for (int i = 0; i < 5; ++i) g[i] = fv[i];
+                } else {
+                    for (int i = 0; i < 5; ++i) g[i] = ov[i] - uc * (ov[i] - fv[i]);
+                }
+                for (int i = 5; i < NF; ++i) g[i] = fv[i];
+            }
+            store_moments<S>(P, P.b, ob, g);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- initial conditions
+struct ICParams {
+    int kind;
+    int h;         // rti interface-normal axis
+    float bc0, bc1, bc2, brad, bwidth, bphase;
+    float rpos, ramp, rwidth, rphase, rk0, rk1;
+};
+
+template <typename S>
+__global__ void init_kernel(const StepParams P, const ICParams I) {
+    const long long total = static_cast<long long>(P.nx) * P.ny * P.nz;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int x = static_cast<int>(e % P.nx);
+        const int y = static_cast<int>((e / P.nx) % P.ny);
+        const int z = static_cast<int>(e / (static_cast<long long>(P.nx) * P.ny));
+        const long long o = lin(P, x, y, z);
+        float m[NF];
+        for (int i = 0; i < NF; ++i) m[i] = 0.0f;
+        if (I.kind == MBCG_IC_JET) {
+            // jet/jetIn.cuh:16-33: ambient fluid at rest everywhere
+            if (P.jet_blue) m[0] = P.rho_r0;
+            else m[1] = P.rho_b0;
+        } else if (I.kind == MBCG_IC_BUBBLE) {
+            // bubble/bubbleIn.cuh:15-52, fluid nodes only
+            if (x == 0 || y == 0 || z == 0 || x == P.nx - 1 || y == P.ny - 1 || z == P.nz - 1) continue;
+            const float dx = __fsub_rn(static_cast<float>(x), I.bc0);
+            const float dy = __fsub_rn(static_cast<float>(y), I.bc1);
+            const float dz = __fsub_rn(static_cast<float>(z), I.bc2);
+            const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            if (I.bwidth <= 0.0f) {
+                const float in = r2 <= __fmul_rn(I.brad, I.brad) ? 1.0f : 0.0f;
+                if (I.bphase < 0.0f) {
+                    m[0] = (1.0f - in) * P.rho_r0;
+                    m[1] = in * P.rho_b0;
+                } else {
+                    m[0] = in * P.rho_r0;
+                    m[1] = (1.0f - in) * P.rho_b0;
+                }
+            } else {
+                const float ps = I.bphase * tanhf((I.brad - sqrtf(r2)) / I.bwidth);
+                m[0] = 0.5f * (1.0f + ps) * P.rho_r0;
+                m[1] = 0.5f * (1.0f - ps) * P.rho_b0;
+            }
+        } else if (I.kind == MBCG_IC_RTI) {
+            // rti/rtiIn.cuh:18-70
+            const int c3[3] = {x, y, z};
+            int t0, t1;
+            transverse(I.h, t0, t1);
+            const float pos = __fadd_rn(I.rpos, __fmul_rn(__fmul_rn(I.ramp, cosf(__fmul_rn(I.rk0, static_cast<float>(c3[t0])))),
+                                                          cosf(__fmul_rn(I.rk1, static_cast<float>(c3[t1])))));
+            const float phi = tanhf(__fdiv_rn(__fsub_rn(static_cast<float>(c3[I.h]), pos), I.rwidth));
+            if (I.rphase < 0.0f) {
+                m[0] = 0.5f * (1.0f - phi) * P.rho_r0;
+                m[1] = 0.5f * (1.0f + phi) * P.rho_b0;
+            } else {
+                m[0] = 0.5f * (1.0f + phi) * P.rho_r0;
+                m[1] = 0.5f * (1.0f - phi) * P.rho_b0;
+            }
+        } else {
+            continue;
+        }
+        store_moments<S>(P, P.b, o, m);
+    }
+}
+
+// rtiIn.cuh:76-119: the interface-normal ghost layers copy their neighbour, u = 0
+template <typename S>
+__global__ void rti_walls_kernel(const StepParams P, int h) {
+    int t0, t1;
+    transverse(h, t0, t1);
+    const int n3[3] = {P.nx, P.ny, P.nz};
+    const int n0 = n3[t0] - 2, n1 = n3[t1] - 2;
+    const long long total = static_cast<long long>(n0) * n1;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int u = 1 + static_cast<int>(e % n0), v = 1 + static_cast<int>(e / n0);
+        for (int side = 0; side < 2; ++side) {
+            int pb[3], pf[3];
+            pb[t0] = pf[t0] = u;
+            pb[t1] = pf[t1] = v;
+            pb[h] = side == 0 ? 0 : n3[h] - 1;
+            pf[h] = side == 0 ? 1 : n3[h] - 2;
+            float fv[NF];
+            load_node<S>(P, P.b, lin(P, pf[0], pf[1], pf[2]), fv);
+            to_moments<S>(P, fv);
+            fv[2] = fv[3] = fv[4] = 0.0f;
+            store_moments<S>(P, P.b, lin(P, pb[0], pb[1], pb[2]), fv);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- diagnostics
+struct DiagParams {
+    int bubble;
+    float c0, c1, c2, r_in2, r_out2;
+    float kappa_r, kappa_b;
+};
+
+template <typename S>
+__global__ void diag_kernel(const StepParams P, const DiagParams D, double* partials) {
+    const long long n0 = P.nx - 2, n1 = P.ny - 2, n2 = P.nz - 2;
+    const long long total = n0 * n1 * n2;
+    double acc[kDiagSlots];
+    for (int i = 0; i < kDiagSlots; ++i) acc[i] = 0.0;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int x = 1 + static_cast<int>(e % n0);
+        const int y = 1 + static_cast<int>((e / n0) % n1);
+        const int z = 1 + static_cast<int>(e / (n0 * n1));
+        float v[NF];
+        load_node<S>(P, P.a, lin(P, x, y, z), v);
+        to_moments<S>(P, v);
+        const double rr = v[0], rb = v[1], rho = rr + rb;
+        bool bad = !(rho > 0.0);
+        for (int i = 0; i < NF; ++i) bad |= !isfinite(v[i]);
+        acc[0] += rr;
+        acc[1] += rb;
+        acc[2] += rho * v[2];
+        acc[3] += rho * v[3];
+        acc[4] += rho * v[4];
+        if (D.bubble) {
+            const float dx = x - D.c0, dy = y - D.c1, dz = z - D.c2;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            const double p = (rho + rr * D.kappa_r + rb * D.kappa_b) / 3.0;
+            if (r2 <= D.r_in2) { acc[5] += p; acc[6] += 1.0; }
+            if (r2 >= D.r_out2) { acc[7] += p; acc[8] += 1.0; }
+        }
+        acc[9] += bad ? 1.0 : 0.0;
+        acc[10] += 1.0;
+    }
+    // block reduction (fixed order: warp shuffles, then warps in index order)
+    __shared__ double red[32][kDiagSlots];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int i = 0; i < kDiagSlots; ++i) {
+        double s = acc[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) red[wid][i] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < kDiagSlots) {
+        double s = 0.0;
+        for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) s += red[wv][threadIdx.x];
+        partials[blockIdx.x * kDiagSlots + threadIdx.x] = s;
+    }
+}
+
+__global__ void diag_final_kernel(const double* partials, int nparts, double* result) {
+    const int i = threadIdx.x;
+    if (i < kDiagSlots) {
+        double s = 0.0;
+        for (int b = 0; b < nparts; ++b) s += partials[b * kDiagSlots + i];
+        result[i] = s;
+    }
+}
+
+// ---------------------------------------------------------------- dense conversions
+template <typename S>
+__global__ void to_dense_kernel(const StepParams P, int field, float* dst) {
+    const long long total = static_cast<long long>(P.nx) * P.ny * P.nz;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int x = static_cast<int>(e % P.nx);
+        const int y = static_cast<int>((e / P.nx) % P.ny);
+        const int z = static_cast<int>(e / (static_cast<long long>(P.nx) * P.ny));
+        const long long o = lin(P, x, y, z);
+        float v;
+        if constexpr (sizeof(S) == 4) {
+            v = static_cast<const float*>(P.a[field])[o];
+        } else {
+            if (field <= 1) {
+                const float s0 = Codec<S>::to_f(static_cast<const S*>(P.a[0])[o]);
+                const float phi = Codec<S>::to_f(static_cast<const S*>(P.a[1])[o]);
+                const float rho = P.rho_mean + phi * P.rho_half_diff + P.rho_scale * s0;
+                v = field == 0 ? 0.5f * rho * (1.0f + phi) : 0.5f * rho * (1.0f - phi);
+            } else {
+                const float s = Codec<S>::to_f(static_cast<const S*>(P.a[field])[o]);
+                v = s * (field < 5 ? P.u_ref : P.pi_scale);
+            }
+        }
+        dst[e] = v;
+    }
+}
+
+// dense FP32 moments (all 11 fields, reference layout) -> stored slots
+template <typename S>
+__global__ void from_dense_kernel(const StepParams P, const float* src) {
+    const long long total = static_cast<long long>(P.nx) * P.ny * P.nz;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int x = static_cast<int>(e % P.nx);
+        const int y = static_cast<int>((e / P.nx) % P.ny);
+        const int z = static_cast<int>(e / (static_cast<long long>(P.nx) * P.ny));
+        float m[NF];
+        for (int i = 0; i < NF; ++i) m[i] = src[i * total + e];
+        if (m[0] + m[1] == 0.0f) {
+            // unused ghost node with no fluid: store zeros rather than 0/0
+            for (int i = 0; i < NF; ++i) static_cast<S*>(P.b[i])[lin(P, x, y, z)] = Codec<S>::from_f(0.0f);
+            continue;
+        }
+        store_moments<S>(P, P.b, lin(P, x, y, z), m);
+    }
+}
+
+template <typename S>
+cudaError_t bc_t(const StepParams& P, int init_inlet, cudaStream_t s) {
+    bc_kernel<S><<<256, 256, 0, s>>>(P, init_inlet);
+    return cudaGetLastError();
+}
+
+int grid_for(long long n) {
+    long long g = (n + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    if (g < 1) g = 1;
+    return static_cast<int>(g);
+}
+
+} // namespace
+
+cudaError_t launch_bc(int precision, const StepParams& P, cudaStream_t s) {
+    if (P.inout_axis < 0) return cudaSuccess;
+    switch (precision) {
+    case MBCG_FP16: return bc_t<__half>(P, 0, s);
+    case MBCG_BF16: return bc_t<__nv_bfloat16>(P, 0, s);
+    default: return bc_t<float>(P, 0, s);
+    }
+}
+
+template <typename S>
+static cudaError_t init_t(const StepParams& P, const mbcg_params& p, cudaStream_t s) {
+    ICParams I{};
+    I.kind = p.ic;
+    I.h = 1;
+    for (int a = 0; a < 3; ++a)
+        if (p.bc[a] == MBCG_BC_WALL) I.h = a;
+    I.bc0 = static_cast<float>(p.bubble_center[0]);
+    I.bc1 = static_cast<float>(p.bubble_center[1]);
+    I.bc2 = static_cast<float>(p.bubble_center[2]);
+    I.brad = static_cast<float>(p.bubble_radius);
+    I.bwidth = static_cast<float>(p.bubble_width);
+    I.bphase = static_cast<float>(p.bubble_phase);
+    I.rpos = static_cast<float>(p.rti_position);
+    I.ramp = static_cast<float>(p.rti_amplitude);
+    I.rwidth = static_cast<float>(p.rti_width);
+    I.rphase = static_cast<float>(p.rti_phase_above);
+    {
+        const int n3[3] = {p.nx, p.ny, p.nz};
+        const int t0 = I.h == 0 ? 1 : 0, t1 = I.h == 2 ? 1 : 2;
+        // rtiIn.cuh:71-84: k = 2 pi mode / (N - 2), evaluated in float as the reference does
+        const float pi = 3.141592653589793f;
+        I.rk0 = 2.0f * pi * static_cast<float>(p.rti_mode[0]) / static_cast<float>(n3[t0] - 2);
+        I.rk1 = 2.0f * pi * static_cast<float>(p.rti_mode[1]) / static_cast<float>(n3[t1] - 2);
+    }
+    const long long n = static_cast<long long>(P.nx) * P.ny * P.nz;
+    init_kernel<S><<<grid_for(n), 256, 0, s>>>(P, I);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (p.ic == MBCG_IC_RTI) {
+        rti_walls_kernel<S><<<256, 256, 0, s>>>(P, I.h);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (p.ic == MBCG_IC_JET && P.inout_axis >= 0) {
+        // jet/jetIn.cuh:39-60 then the initial boundary pass with B = A (main.cu:25-26)
+        StepParams Q = P;
+        Q.a[0] = nullptr;
+        for (int i = 0; i < NF; ++i) Q.a[i] = P.b[i];
+        Q.step = 0;
+        e = bc_t<S>(Q, 1, s);
+        if (e != cudaSuccess) return e;
+        e = bc_t<S>(Q, 0, s);
+    }
+    return e;
+}
+
+cudaError_t launch_init(int precision, const StepParams& P, const mbcg_params& p, cudaStream_t s) {
+    switch (precision) {
+    case MBCG_FP16: return init_t<__half>(P, p, s);
+    case MBCG_BF16: return init_t<__nv_bfloat16>(P, p, s);
+    default: return init_t<float>(P, p, s);
+    }
+}
+
+int diag_partials_needed(const StepParams& P) {
+    return grid_for(static_cast<long long>(P.nx - 2) * (P.ny - 2) * (P.nz - 2));
+}
+
+template <typename S>
+static cudaError_t diag_t(const StepParams& P, const mbcg_params& p, double* partials, int nparts, double* result,
+                          cudaStream_t s) {
+    DiagParams D{};
+    D.bubble = p.ic == MBCG_IC_BUBBLE;
+    D.c0 = static_cast<float>(p.bubble_center[0]);
+    D.c1 = static_cast<float>(p.bubble_center[1]);
+    D.c2 = static_cast<float>(p.bubble_center[2]);
+    const float rin = 0.5f * static_cast<float>(p.bubble_radius);
+    const float rout = static_cast<float>(p.bubble_radius + 2.0 * p.bubble_width + 4.0);
+    D.r_in2 = rin * rin;
+    D.r_out2 = rout * rout;
+    D.kappa_r = P.ratio ? P.kappa_r : 0.0f;
+    D.kappa_b = P.ratio ? P.kappa_b : 0.0f;
+    diag_kernel<S><<<nparts, 256, 0, s>>>(P, D, partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    diag_final_kernel<<<1, 32, 0, s>>>(partials, nparts, result);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_diag(int precision, const StepParams& P, const mbcg_params& p, double* partials, int nparts,
+                        double* result, cudaStream_t s) {
+    switch (precision) {
+    case MBCG_FP16: return diag_t<__half>(P, p, partials, nparts, result, s);
+    case MBCG_BF16: return diag_t<__nv_bfloat16>(P, p, partials, nparts, result, s);
+    default: return diag_t<float>(P, p, partials, nparts, result, s);
+    }
+}
+
+cudaError_t launch_to_dense(int precision, const StepParams& P, int field, const void* src, float* dst,
+                            cudaStream_t s) {
+    (void)src;
+    const long long n = static_cast<long long>(P.nx) * P.ny * P.nz;
+    switch (precision) {
+    case MBCG_FP16: to_dense_kernel<__half><<<grid_for(n), 256, 0, s>>>(P, field, dst); break;
+    case MBCG_BF16: to_dense_kernel<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>(P, field, dst); break;
+    default: to_dense_kernel<float><<<grid_for(n), 256, 0, s>>>(P, field, dst); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_dense(int precision, const StepParams& P, int field, const float* src, void* dst,
+                              cudaStream_t s) {
+    (void)field;
+    (void)dst;
+    const long long n = static_cast<long long>(P.nx) * P.ny * P.nz;
+    switch (precision) {
+    case MBCG_FP16: from_dense_kernel<__half><<<grid_for(n), 256, 0, s>>>(P, src); break;
+    case MBCG_BF16: from_dense_kernel<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>(P, src); break;
+    default: from_dense_kernel<float><<<grid_for(n), 256, 0, s>>>(P, src); break;
+    }
+    return cudaGetLastError();
+}
+
+} // namespace mbcg

@@ -1,0 +1,560 @@
+// mbcg_capi.cu -- the extern "C" boundary of libmbcg.so (declared in include/mbcg.h).
+//
+// Replaces the reference's host layer: allocate_device_memory / free_device_memory
+// (memory.cuh:153-194), launch_RCS / launch_JetBoundaryConditions / launch_Init*
+// (launch.cuh:14-94), swap_moments (memory.cuh:200-203) and copy_out_D2H
+// (memory.cuh:209-217).  Errors are returned as status codes with a per-thread message,
+// never by exit() (utilities/cudaUtilities.cuh:9-19).
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "mbcg_internal.h"
+
+using namespace mbcg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MBCG_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define MBCG_TRY(call, what)                          \
+    do {                                              \
+        cudaError_t e__ = (call);                     \
+        if (e__ != cudaSuccess) return cuda_fail(e__, what); \
+    } while (0)
+
+int elem_bytes(int precision) { return precision == MBCG_FP32 ? 4 : 2; }
+
+int validate(const mbcg_params* p) {
+    if (!p) return fail(MBCG_E_INVALID, "null parameters");
+    if (p->q != 19 && p->q != 27) return fail(MBCG_E_INVALID, "q must be 19 or 27");
+    if (p->nx < 4 || p->ny < 4 || p->nz < 4) return fail(MBCG_E_INVALID, "each lattice axis needs >= 4 nodes");
+    if (static_cast<long long>(p->nx) * p->ny * p->nz >= (1LL << 40))
+        return fail(MBCG_E_INVALID, "lattice too large");
+    int nonper = 0;
+    for (int a = 0; a < 3; ++a) {
+        if (p->bc[a] < MBCG_BC_PERIODIC || p->bc[a] > MBCG_BC_WALL) return fail(MBCG_E_INVALID, "unknown boundary kind");
+        if (p->bc[a] != MBCG_BC_PERIODIC) ++nonper;
+    }
+    if (nonper > 1) return fail(MBCG_E_INVALID, "at most one axis may be non-periodic");
+    if (p->precision < MBCG_FP32 || p->precision > MBCG_BF16) return fail(MBCG_E_INVALID, "unknown precision");
+    if (!(p->tau > 0.5)) return fail(MBCG_E_INVALID, "tau must exceed 1/2");
+    if (!(p->rho_r0 > 0.0) || !(p->rho_b0 > 0.0)) return fail(MBCG_E_INVALID, "phase densities must be positive");
+    if (p->precision != MBCG_FP32 && (!(p->rho_scale > 0) || !(p->u_ref > 0) || !(p->pi_scale > 0)))
+        return fail(MBCG_E_INVALID, "FP16/BF16 storage needs positive rho_scale, u_ref and pi_scale");
+    return MBCG_OK;
+}
+
+int inout_axis(const mbcg_params& p) {
+    for (int a = 0; a < 3; ++a)
+        if (p.bc[a] == MBCG_BC_INOUT) return a;
+    return -1;
+}
+
+// the reference's float constant chain (constants.cuh:56-93, forces.cuh:114-117)
+void fill_physics(const mbcg_params& p, StepParams& P) {
+    std::memset(&P, 0, sizeof(P));
+    P.nx = p.nx;
+    P.ny = p.ny;
+    P.nz = p.nz;
+    for (int a = 0; a < 3; ++a) P.bc[a] = p.bc[a];
+    P.inout_axis = inout_axis(p);
+    P.outlet = p.outlet;
+    const float taub = static_cast<float>(p.tau);
+    P.oms = 1.0f - 1.0f / taub;
+    const float cs2 = static_cast<float>(1.0 / 3.0);
+    const float cs4 = cs2 * cs2;
+    const float s4 = static_cast<float>(p.sigma) / (4.0f * cs4);
+    P.A = s4 / taub;
+    P.beta = static_cast<float>(p.beta);
+    P.ratio = p.rho_r0 != p.rho_b0;
+    const double rmin = std::min(p.rho_r0, p.rho_b0);
+    P.kappa_r = static_cast<float>(rmin / p.rho_r0 - 1.0);
+    P.kappa_b = static_cast<float>(rmin / p.rho_b0 - 1.0);
+    P.forced = p.gravity[0] != 0.0 || p.gravity[1] != 0.0 || p.gravity[2] != 0.0;
+    for (int a = 0; a < 3; ++a) P.g[a] = static_cast<float>(p.gravity[a]);
+    P.jet_c0 = static_cast<float>(p.jet_center[0]);
+    P.jet_c1 = static_cast<float>(p.jet_center[1]);
+    P.jet_radius = static_cast<float>(p.jet_radius);
+    P.jet_velocity = static_cast<float>(p.jet_velocity);
+    P.noise_amp = static_cast<float>(p.jet_velocity * p.inlet_noise);
+    P.jet_blue = p.jet_phase < 0.0;
+    P.rho_r0 = static_cast<float>(p.rho_r0);
+    P.rho_b0 = static_cast<float>(p.rho_b0);
+    P.seed = p.seed;
+    P.rho_scale = static_cast<float>(p.rho_scale);
+    P.inv_rho_scale = p.rho_scale > 0 ? static_cast<float>(1.0 / p.rho_scale) : 0.0f;
+    P.u_ref = static_cast<float>(p.u_ref);
+    P.inv_u_ref = p.u_ref > 0 ? static_cast<float>(1.0 / p.u_ref) : 0.0f;
+    P.pi_scale = static_cast<float>(p.pi_scale);
+    P.inv_pi_scale = p.pi_scale > 0 ? static_cast<float>(1.0 / p.pi_scale) : 0.0f;
+    P.rho_mean = static_cast<float>(0.5 * (p.rho_r0 + p.rho_b0));
+    P.rho_half_diff = static_cast<float>(0.5 * (p.rho_r0 - p.rho_b0));
+    P.do_bc = 1;
+}
+
+int choose_zchunk(const mbcg_params& p) {
+    if (const char* env = std::getenv("MBCG_ZCHUNK")) {
+        const int v = std::atoi(env);
+        if (v > 0) return v;
+    }
+    const int W = step_box_rows();
+    const long long gx = (p.nx - 2 + step_tile_x() - 1) / step_tile_x();
+    const long long gy = (p.ny - 2 + W - 3) / (W - 2);
+    const int nzf = p.nz - 2;
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // aim for about four waves of one CTA per SM, with at least 16 planes per chunk
+    const long long want = 4LL * sms;
+    long long gz = (want + gx * gy - 1) / (gx * gy);
+    gz = std::max<long long>(1, std::min<long long>(gz, std::max(1, nzf / 16)));
+    return static_cast<int>((nzf + gz - 1) / gz);
+}
+
+// ---------------------------------------------------------------- tensor maps
+using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                              const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeFn get_encode() {
+    static EncodeFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeFn>(ptr);
+    });
+    return fn;
+}
+
+bool tma_capable(const mbcg_params& p, const void* const* f, long long pitch, int precision) {
+    if (std::getenv("MBCG_NO_TMA")) return false;
+    const int es = elem_bytes(precision);
+    if ((pitch * es) % 16 != 0) return false;
+    for (int i = 0; i < NF; ++i)
+        if (reinterpret_cast<uintptr_t>(f[i]) % 16 != 0) return false;
+    return get_encode() != nullptr;
+}
+
+int encode_maps(const mbcg_params& p, const void* const* f, long long pitch, int precision, TensorMaps& T) {
+    EncodeFn enc = get_encode();
+    if (!enc) return fail(MBCG_E_CUDA, "cuTensorMapEncodeTiled unavailable");
+    const int es = elem_bytes(precision);
+    const int W = step_box_rows();
+    for (int i = 0; i < NF; ++i) {
+        const cuuint64_t dims[3] = {static_cast<cuuint64_t>(p.nx), static_cast<cuuint64_t>(p.ny),
+                                    static_cast<cuuint64_t>(p.nz)};
+        const cuuint64_t strides[2] = {static_cast<cuuint64_t>(pitch * es),
+                                       static_cast<cuuint64_t>(pitch * p.ny * es)};
+        const cuuint32_t box[3] = {static_cast<cuuint32_t>(i < 2 ? step_rb_box_x() : step_m_box_x()),
+                                   static_cast<cuuint32_t>(i < 2 ? W + 2 : W), 1u};
+        const cuuint32_t estr[3] = {1u, 1u, 1u};
+        const CUresult r = enc(&T.m[i], es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3,
+                               const_cast<void*>(f[i]), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(MBCG_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(r) + ")");
+    }
+    return MBCG_OK;
+}
+
+} // namespace
+
+struct mbcg_case {
+    mbcg_params p;
+    int es = 4;
+    long long pitch = 0, plane = 0, fstride = 0;
+    void* buf[2] = {nullptr, nullptr};
+    void* fields[2][NF] = {};
+    int cur = 0;
+    bool tma = false;
+    TensorMaps tm[2];
+    int* status = nullptr;
+    double* diag_partials = nullptr;
+    double* diag_result = nullptr;
+    int nparts = 0;
+    long long steps = 0;
+    int zchunk = 16;
+};
+
+namespace {
+
+StepParams make_params(const mbcg_case* c, int from, long long step) {
+    StepParams P;
+    fill_physics(c->p, P);
+    P.pitch = c->pitch;
+    P.plane = c->plane;
+    P.zchunk = c->zchunk;
+    P.status = c->status;
+    P.step = step;
+    for (int i = 0; i < NF; ++i) {
+        P.a[i] = c->fields[from][i];
+        P.b[i] = c->fields[from ^ 1][i];
+    }
+    return P;
+}
+
+void free_case(mbcg_case* c) {
+    if (!c) return;
+    for (int s = 0; s < 2; ++s)
+        if (c->buf[s]) cudaFree(c->buf[s]);
+    if (c->status) cudaFree(c->status);
+    if (c->diag_partials) cudaFree(c->diag_partials);
+    if (c->diag_result) cudaFree(c->diag_result);
+    delete c;
+}
+
+int* g_raw_status = nullptr; // status word of the raw entry points, allocated once per process
+std::mutex g_raw_mu;
+
+int* raw_status() {
+    std::lock_guard<std::mutex> lk(g_raw_mu);
+    if (!g_raw_status) {
+        if (cudaMalloc(&g_raw_status, sizeof(int)) != cudaSuccess) {
+            g_raw_status = nullptr;
+            return nullptr;
+        }
+        cudaMemset(g_raw_status, 0, sizeof(int));
+    }
+    return g_raw_status;
+}
+
+int check_view(const mbcg_params* p, const mbcg_moments* m) {
+    if (!m) return fail(MBCG_E_INVALID, "null moments view");
+    if (m->precision != p->precision) return fail(MBCG_E_INVALID, "moments precision differs from params");
+    if (m->pitch < p->nx) return fail(MBCG_E_INVALID, "pitch smaller than nx");
+    for (int i = 0; i < NF; ++i)
+        if (!m->f[i]) return fail(MBCG_E_INVALID, "null field pointer");
+    return MBCG_OK;
+}
+
+StepParams raw_params(const mbcg_params* p, const mbcg_moments* a, const mbcg_moments* b, long long step) {
+    StepParams P;
+    fill_physics(*p, P);
+    P.pitch = b ? b->pitch : a->pitch;
+    P.plane = P.pitch * p->ny;
+    P.zchunk = choose_zchunk(*p);
+    P.step = step;
+    P.status = raw_status();
+    for (int i = 0; i < NF; ++i) {
+        P.a[i] = a ? a->f[i] : nullptr;
+        P.b[i] = b ? b->f[i] : nullptr;
+    }
+    return P;
+}
+
+} // namespace
+
+extern "C" {
+
+void mbcg_params_default(mbcg_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->q = 27;
+    p->nx = p->ny = p->nz = 128;
+    p->bc[0] = MBCG_BC_PERIODIC;
+    p->bc[1] = MBCG_BC_INOUT;
+    p->bc[2] = MBCG_BC_PERIODIC;
+    p->outlet = MBCG_OUTLET_CONVECTIVE;
+    p->precision = MBCG_FP32;
+    p->ic = MBCG_IC_JET;
+    p->tau = 1.0;
+    p->sigma = 0.1;
+    p->beta = 0.9;
+    p->rho_r0 = p->rho_b0 = 1.0;
+    p->jet_radius = 12.0;
+    p->jet_velocity = 0.05;
+    p->jet_center[0] = (p->nx - 1) / 2.0;
+    p->jet_center[1] = (p->nz - 1) / 2.0;
+    p->jet_phase = -1.0;
+    p->seed = 12345;
+    p->bubble_radius = 30.0;
+    for (int a = 0; a < 3; ++a) p->bubble_center[a] = (127) / 2.0;
+    p->bubble_phase = -1.0;
+    p->rti_position = (p->ny - 1) / 2.0;
+    p->rti_amplitude = 4.0;
+    p->rti_width = 4.0;
+    p->rti_phase_above = -1.0;
+    p->rti_mode[0] = p->rti_mode[1] = 1;
+    p->rho_scale = 0.01;
+    p->u_ref = 0.05;
+    p->pi_scale = 0.05 * 0.05;
+}
+
+int mbcg_create(const mbcg_params* p, mbcg_case** out) {
+    if (!out) return fail(MBCG_E_INVALID, "null output handle");
+    *out = nullptr;
+    if (int rc = validate(p)) return rc;
+    mbcg_case* c = new mbcg_case();
+    c->p = *p;
+    c->es = elem_bytes(p->precision);
+    c->pitch = (p->nx + 7) / 8 * 8;
+    c->plane = c->pitch * p->ny;
+    const long long per_field = c->plane * p->nz;
+    c->fstride = (per_field * c->es + 255) / 256 * 256 / c->es;
+    const size_t bytes = static_cast<size_t>(c->fstride) * NF * c->es;
+    for (int s = 0; s < 2; ++s) {
+        cudaError_t e = cudaMalloc(&c->buf[s], bytes);
+        if (e != cudaSuccess) {
+            free_case(c);
+            return fail(MBCG_E_NOMEM, std::string("cudaMalloc of a moment state failed: ") + cudaGetErrorString(e));
+        }
+        cudaMemset(c->buf[s], 0, bytes);
+        for (int i = 0; i < NF; ++i)
+            c->fields[s][i] = static_cast<unsigned char*>(c->buf[s]) + static_cast<size_t>(i) * c->fstride * c->es;
+    }
+    if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) {
+        free_case(c);
+        return fail(MBCG_E_NOMEM, "cudaMalloc of the status word failed");
+    }
+    cudaMemset(c->status, 0, sizeof(int));
+    c->zchunk = choose_zchunk(*p);
+    {
+        StepParams P = make_params(c, 0, 0);
+        c->nparts = diag_partials_needed(P);
+    }
+    if (cudaMalloc(&c->diag_partials, sizeof(double) * kDiagSlots * c->nparts) != cudaSuccess ||
+        cudaMalloc(&c->diag_result, sizeof(double) * kDiagSlots) != cudaSuccess) {
+        free_case(c);
+        return fail(MBCG_E_NOMEM, "cudaMalloc of the diagnostics buffers failed");
+    }
+    c->tma = tma_capable(*p, c->fields[0], c->pitch, p->precision) &&
+             tma_capable(*p, c->fields[1], c->pitch, p->precision);
+    if (c->tma) {
+        for (int s = 0; s < 2; ++s)
+            if (int rc = encode_maps(*p, c->fields[s], c->pitch, p->precision, c->tm[s])) {
+                free_case(c);
+                return rc;
+            }
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        free_case(c);
+        return cuda_fail(e, "mbcg_create");
+    }
+    *out = c;
+    return MBCG_OK;
+}
+
+int mbcg_destroy(mbcg_case* c) {
+    if (!c) return MBCG_OK;
+    cudaDeviceSynchronize();
+    free_case(c);
+    return MBCG_OK;
+}
+
+int mbcg_init(mbcg_case* c, mbcg_stream_t s) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    StepParams P = make_params(c, c->cur ^ 1, 0); // P.b = current state A
+    MBCG_TRY(launch_init(c->p.precision, P, c->p, reinterpret_cast<cudaStream_t>(s)), "initial condition");
+    c->steps = 0;
+    return MBCG_OK;
+}
+
+int mbcg_step(mbcg_case* c, int32_t nsteps, mbcg_stream_t s) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    if (nsteps < 0) return fail(MBCG_E_INVALID, "negative step count");
+    for (int n = 0; n < nsteps; ++n) {
+        StepParams P = make_params(c, c->cur, c->steps + 1);
+        MBCG_TRY(launch_step(c->p.q, c->p.precision, c->tma, P, c->tm[c->cur], reinterpret_cast<cudaStream_t>(s)),
+                 "step kernel");
+        c->cur ^= 1;
+        c->steps += 1;
+    }
+    return MBCG_OK;
+}
+
+int mbcg_rcs(mbcg_case* c, mbcg_stream_t s) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    StepParams P = make_params(c, c->cur, c->steps + 1);
+    P.do_bc = 0;
+    MBCG_TRY(launch_step(c->p.q, c->p.precision, c->tma, P, c->tm[c->cur], reinterpret_cast<cudaStream_t>(s)),
+             "RCS kernel");
+    return MBCG_OK;
+}
+
+int mbcg_bc(mbcg_case* c, mbcg_stream_t s) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    StepParams P = make_params(c, c->cur, c->steps + 1); // a = old state, b = new state
+    MBCG_TRY(launch_bc(c->p.precision, P, reinterpret_cast<cudaStream_t>(s)), "boundary kernel");
+    return MBCG_OK;
+}
+
+int mbcg_swap(mbcg_case* c) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    c->cur ^= 1;
+    c->steps += 1;
+    return MBCG_OK;
+}
+
+int mbcg_fields(const mbcg_case* c, mbcg_moments* a, mbcg_moments* b) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    for (int w = 0; w < 2; ++w) {
+        mbcg_moments* m = w == 0 ? a : b;
+        if (!m) continue;
+        const int s = w == 0 ? c->cur : (c->cur ^ 1);
+        for (int i = 0; i < NF; ++i) m->f[i] = c->fields[s][i];
+        m->pitch = c->pitch;
+        m->precision = c->p.precision;
+        m->reserved = 0;
+    }
+    return MBCG_OK;
+}
+
+int64_t mbcg_steps_done(const mbcg_case* c) { return c ? c->steps : -1; }
+
+int mbcg_copy_out(mbcg_case* c, float* const host[MBCG_NFIELDS], mbcg_stream_t s) {
+    if (!c || !host) return fail(MBCG_E_INVALID, "null argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+    const mbcg_params& p = c->p;
+    const size_t row = static_cast<size_t>(p.nx) * sizeof(float);
+    const size_t rows = static_cast<size_t>(p.ny) * p.nz;
+    if (p.precision == MBCG_FP32) {
+        for (int i = 0; i < NF; ++i)
+            MBCG_TRY(cudaMemcpy2DAsync(host[i], row, c->fields[c->cur][i], c->pitch * sizeof(float), row, rows,
+                                       cudaMemcpyDeviceToHost, st),
+                     "copy out");
+    } else {
+        float* staging = nullptr;
+        const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
+        MBCG_TRY(cudaMalloc(&staging, n * sizeof(float)), "staging allocation");
+        StepParams P = make_params(c, c->cur, c->steps);
+        for (int i = 0; i < NF; ++i) {
+            cudaError_t e = launch_to_dense(p.precision, P, i, nullptr, staging, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(host[i], staging, n * sizeof(float), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                cudaFree(staging);
+                return cuda_fail(e, "copy out");
+            }
+        }
+        cudaFree(staging);
+    }
+    MBCG_TRY(cudaStreamSynchronize(st), "copy out");
+    return MBCG_OK;
+}
+
+int mbcg_copy_in(mbcg_case* c, const float* const host[MBCG_NFIELDS], mbcg_stream_t s) {
+    if (!c || !host) return fail(MBCG_E_INVALID, "null argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+    const mbcg_params& p = c->p;
+    const size_t row = static_cast<size_t>(p.nx) * sizeof(float);
+    const size_t rows = static_cast<size_t>(p.ny) * p.nz;
+    if (p.precision == MBCG_FP32) {
+        for (int i = 0; i < NF; ++i)
+            MBCG_TRY(cudaMemcpy2DAsync(c->fields[c->cur][i], c->pitch * sizeof(float), host[i], row, row, rows,
+                                       cudaMemcpyHostToDevice, st),
+                     "copy in");
+    } else {
+        float* staging = nullptr;
+        const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
+        MBCG_TRY(cudaMalloc(&staging, NF * n * sizeof(float)), "staging allocation");
+        cudaError_t e = cudaSuccess;
+        for (int i = 0; i < NF && e == cudaSuccess; ++i)
+            e = cudaMemcpyAsync(staging + i * n, host[i], n * sizeof(float), cudaMemcpyHostToDevice, st);
+        StepParams P = make_params(c, c->cur ^ 1, c->steps); // P.b = current state
+        if (e == cudaSuccess) e = launch_from_dense(p.precision, P, 0, staging, nullptr, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(staging);
+        if (e != cudaSuccess) return cuda_fail(e, "copy in");
+    }
+    MBCG_TRY(cudaStreamSynchronize(st), "copy in");
+    return MBCG_OK;
+}
+
+int mbcg_diagnostics(mbcg_case* c, mbcg_diag* out, mbcg_stream_t s) {
+    if (!c || !out) return fail(MBCG_E_INVALID, "null argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+    StepParams P = make_params(c, c->cur, c->steps);
+    MBCG_TRY(launch_diag(c->p.precision, P, c->p, c->diag_partials, c->nparts, c->diag_result, st), "diagnostics");
+    double r[kDiagSlots];
+    MBCG_TRY(cudaMemcpyAsync(r, c->diag_result, sizeof(r), cudaMemcpyDeviceToHost, st), "diagnostics copy");
+    MBCG_TRY(cudaStreamSynchronize(st), "diagnostics");
+    out->mass_r = r[0];
+    out->mass_b = r[1];
+    out->momentum[0] = r[2];
+    out->momentum[1] = r[3];
+    out->momentum[2] = r[4];
+    out->p_in = r[6] > 0 ? r[5] / r[6] : 0.0;
+    out->p_out = r[8] > 0 ? r[7] / r[8] : 0.0;
+    out->dp = out->p_in - out->p_out;
+    out->nonfinite = static_cast<int64_t>(r[9]);
+    out->nodes = static_cast<int64_t>(r[10]);
+    return MBCG_OK;
+}
+
+int mbcg_status(mbcg_case* c, int32_t* status) {
+    if (!c || !status) return fail(MBCG_E_INVALID, "null argument");
+    int v = 0;
+    MBCG_TRY(cudaMemcpy(&v, c->status, sizeof(int), cudaMemcpyDeviceToHost), "status read");
+    MBCG_TRY(cudaMemset(c->status, 0, sizeof(int)), "status clear");
+    *status = v;
+    return MBCG_OK;
+}
+
+int mbcg_rcs_moments(const mbcg_params* p, const mbcg_moments* a, const mbcg_moments* b, int64_t step,
+                     mbcg_stream_t s) {
+    if (int rc = validate(p)) return rc;
+    if (int rc = check_view(p, a)) return rc;
+    if (int rc = check_view(p, b)) return rc;
+    if (a->pitch != b->pitch) return fail(MBCG_E_INVALID, "A and B must share a pitch");
+    StepParams P = raw_params(p, a, b, step);
+    P.do_bc = 0;
+    TensorMaps T;
+    std::memset(&T, 0, sizeof(T));
+    const bool tma = tma_capable(*p, a->f, a->pitch, p->precision);
+    if (tma)
+        if (int rc = encode_maps(*p, a->f, a->pitch, p->precision, T)) return rc;
+    MBCG_TRY(launch_step(p->q, p->precision, tma, P, T, reinterpret_cast<cudaStream_t>(s)), "RCS kernel");
+    return MBCG_OK;
+}
+
+int mbcg_bc_moments(const mbcg_params* p, const mbcg_moments* b, const mbcg_moments* a_old, int64_t step,
+                    mbcg_stream_t s) {
+    if (int rc = validate(p)) return rc;
+    if (int rc = check_view(p, b)) return rc;
+    if (int rc = check_view(p, a_old)) return rc;
+    if (a_old->pitch != b->pitch) return fail(MBCG_E_INVALID, "A and B must share a pitch");
+    StepParams P = raw_params(p, a_old, b, step);
+    MBCG_TRY(launch_bc(p->precision, P, reinterpret_cast<cudaStream_t>(s)), "boundary kernel");
+    return MBCG_OK;
+}
+
+int mbcg_init_moments(const mbcg_params* p, const mbcg_moments* a, mbcg_stream_t s) {
+    if (int rc = validate(p)) return rc;
+    if (int rc = check_view(p, a)) return rc;
+    StepParams P = raw_params(p, nullptr, a, 0);
+    MBCG_TRY(launch_init(p->precision, P, *p, reinterpret_cast<cudaStream_t>(s)), "initial condition");
+    return MBCG_OK;
+}
+
+int64_t mbcg_active_nodes(const mbcg_params* p) {
+    if (!p) return -1;
+    return static_cast<int64_t>(p->nx - 2) * (p->ny - 2) * (p->nz - 2);
+}
+
+int32_t mbcg_launches_per_step(const mbcg_case* c) { return c ? 1 : 0; }
+
+const char* mbcg_last_error(void) { return g_err.c_str(); }
+
+const char* mbcg_version(void) { return "mbcg 0.1 (sm_103a)"; }
+
+} // extern "C"
