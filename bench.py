@@ -1,0 +1,312 @@
+"""Benchmark of the fused colour-gradient LBM step on one GB300 (MLUPS, HBM roofline).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload: the D3Q27 liquid jet, 256 x 256 x 1024 fluid nodes (258 x 258 x 1026 lattice
+with the ghost frame), inlet disc of diameter 32 at u_z = 0.05 with +-1% seeded noise,
+periodic x/y, zero-gradient outflow, tau = 0.51, sigma = 1e-3, FP32 moments.  Synthetic
+inputs: the case's own analytic initial condition (no dataset is involved).
+
+One "step" is one time step of the whole lattice (one fused kernel launch).  MLUPS counts
+the fluid nodes (nx-2)(ny-2)(nz-2) per step as the reference's MlupsCounter does
+(utilities/mlups_count.cuh:24-29).  The state (2 x 2.95 GB) is far larger than the 129 MB
+L2, so no explicit L2 flush is needed between timed steps.
+
+--impl reference times the reference algorithm on the host cores instead: the CPU oracle's
+FP32 restatement of the reference step (bit-exact with the reference's own code on the
+golden fixtures), all host threads, on a z-slab sample of the same jet.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lightweight-mb-color-gradient-lbm_gb300")
+sys.path.insert(0, PKG)
+
+import numpy as np  # noqa: E402
+
+import mbcg  # noqa: E402
+
+METRIC = "MLUPS & % of HBM roofline vs plain FP32; serving cases/s, p50/p99 at stated error"
+BYTES_PER_NODE = {mbcg.FP32: 88, mbcg.FP16: 44, mbcg.BF16: 44}
+WORKLOAD = "D3Q27 liquid jet 256x256x1024 fluid nodes (tau 0.51, sigma 1e-3, d=32 inlet, 1% noise)"
+
+
+def jet_workload(precision=mbcg.FP32, nz: int = 1024) -> mbcg.Params:
+    return mbcg.jet_params(256, 256, nz, q=27, precision=precision)
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel_tag: str):
+    """DRAM bytes per launch from the committed ncu summary (profiles/<tag>.txt), if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch_full:"):
+                try:
+                    return float(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        self.out.flush()
+
+    def summary(self) -> dict:
+        try:
+            with open(self.out.name) as f:
+                rows = [r.strip().split(",") for r in f if r.strip()]
+        except Exception:
+            rows = []
+        finally:
+            try:
+                os.unlink(self.out.name)
+            except OSError:
+                pass
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_device(case: mbcg.Case, steps: int, warmup: int, torch):
+    """CUDA-event time of `steps` fused steps on the launching stream (state resident)."""
+    stream = torch.cuda.current_stream()
+    case.step(warmup, stream)
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    case.step(steps, stream)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(stop) / 1000.0
+
+
+def time_e2e(p: mbcg.Params, steps: int, torch) -> dict:
+    """End to end through the C ABI from pinned host memory: per step, copy the state in
+    (H2D), one fused step, copy the state out (D2H)."""
+    shape = (mbcg.NFIELDS,) + p.shape
+    host_in = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+    host_out = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+    with mbcg.Case(p) as c:
+        c.init()
+        c.copy_out(out=host_in.numpy())
+        c.copy_in(host_in.numpy())
+        c.step(1)
+        c.copy_out(out=host_out.numpy())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            c.copy_in(host_in.numpy())
+            c.step(1)
+            c.copy_out(out=host_out.numpy())
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    nbytes = host_in.numel() * 4
+    return {"value": p.active_nodes() * steps / dt / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes, "steps": steps}
+
+
+def cpu_sample_params() -> mbcg.Params:
+    """z-slab of the jet workload (same x/y extent and boundary kinds, 32 fluid planes)."""
+    return mbcg.jet_params(256, 256, 32, q=27)
+
+
+def cpu_leg(budget_s: float, threads: int, real_bytes: int = 4) -> dict:
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    p = cpu_sample_params()
+    dtype = np.float32 if real_bytes == 4 else np.float64
+    a = ol.oracle_init(p, dtype)
+    b = a.copy()
+    ol.oracle_step(p, a, 1, threads=threads, b=b)  # warm
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        ol.oracle_step(p, a, steps + 2, threads=threads, b=b)
+        a, b = b, a
+        steps += 1
+        dt = time.perf_counter() - t0
+        if dt >= budget_s:
+            break
+    return {"value": p.active_nodes() * steps / dt / 1e6, "unit": "MLUPS", "cores": threads,
+            "kind": "port", "sample": f"{steps} step(s) of a 256x256x32-fluid-node z-slab of the jet, "
+                                      f"{'FP32' if real_bytes == 4 else 'FP64'} oracle, {dt:.1f} s"}
+
+
+def reference_arm(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    budget = float(os.environ.get("MBCG_REF_BUDGET_S", "8"))
+    vals = []
+    leg = None
+    for _ in range(max(args.warmup, 0)):
+        cpu_leg(min(budget, 2.0), threads)
+    for _ in range(max(args.steps, 1)):
+        leg = cpu_leg(budget, threads)
+        vals.append(leg["value"])
+    v = statistics.median(vals)
+    slab = cpu_sample_params()
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": slab.active_nodes() / v / 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (analytic jet initial condition)",
+           "config": {"workload": WORKLOAD, "sample": "256x256x32 z-slab per step", "host_threads": threads},
+           "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": threads, "kind": "port",
+                            "sample": leg["sample"] if leg else ""},
+           "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--forms", default="fp16,bf16")
+    ap.add_argument("--nz", type=int, default=1024, help="fluid planes of the jet (profiling uses fewer)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    p = jet_workload(mbcg.FP32, args.nz)
+    peak, peak_kind = measured_peak_hbm()
+    with mbcg.Case(p) as case:
+        case.init()
+        launches = case.launches_per_step()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            dt = time_device(case, args.steps, args.warmup, torch)
+        diag = case.diagnostics()
+        status = case.status()
+    if world > 1:
+        t = torch.tensor([dt], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+    nodes = p.active_nodes()
+    mlups = world * nodes * args.steps / dt / 1e6
+    per_launch = dt / (args.steps * launches)
+    achieved = BYTES_PER_NODE[mbcg.FP32] * nodes / per_launch / 1e9
+    traffic = profiled_traffic("step_kernel_jet256_fp32")
+
+    forms = {}
+    for name in [f for f in args.forms.split(",") if f]:
+        prec = {"fp16": mbcg.FP16, "bf16": mbcg.BF16}[name]
+        q = jet_workload(prec, args.nz)
+        with mbcg.Case(q) as c:
+            c.init()
+            t = time_device(c, args.steps, args.warmup, torch)
+        v = nodes * args.steps / t / 1e6
+        forms[name] = {"value": v, "unit": "MLUPS", "vs_fp32": v / (mlups / world),
+                       "roofline_frac": BYTES_PER_NODE[prec] * nodes / (t / args.steps) / 1e9 / peak}
+
+    e2e = time_e2e(p, args.e2e_steps, torch) if rank == 0 and args.e2e_steps > 0 else None
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_leg(args.cpu_budget, os.cpu_count() or 1)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (analytic jet initial condition, seeded inlet noise)",
+            "config": {"workload": WORKLOAD if args.nz == 1024 else WORKLOAD.replace("x1024", f"x{args.nz}"), "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": nodes,
+                       "precision": "fp32 moments", "l2": "state 2x2.95 GB > 129 MB L2, no flush needed",
+                       "parallelism": "replicas" if world > 1 else "single GPU", "zchunk": os.environ.get("MBCG_ZCHUNK", "auto")},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_node": BYTES_PER_NODE[mbcg.FP32]},
+            "forms": forms,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps * launches,
+            "clocks": clk.summary(),
+            "checks": {"mass_r": diag["mass_r"], "mass_b": diag["mass_b"], "nonfinite": diag["nonfinite"],
+                       "status": status},
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -565,9 +565,11 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
                     cf.p110 += 2.0f * qf * Fx * Fy;
                     cf.p101 += 2.0f * qf * Fx * Fz;
                     cf.p011 += 2.0f * qf * Fy * Fz;
-                    // recolouring (collisionOperators.cuh:60-80): beta rr rb / (rho |F|)
+                    // recolouring (collisionOperators.cuh:60-80): beta rr rb / (rho |F|); with a
+                    // density ratio the rest equilibrium of moving directions is w (rho + K)
                     const float rho = nd.rr + nd.rb;
-                    dcoef = P.beta * (nd.rr * nd.rb) / (rho * absF);
+                    const float feq0 = P.ratio ? rho + nd.rr * P.kappa_r + nd.rb * P.kappa_b : rho;
+                    dcoef = P.beta * (nd.rr * nd.rb) / (rho * rho * absF) * feq0;
                 }
             }
         }

@@ -269,13 +269,14 @@ struct Oracle {
         const R dot = Fx * k.c[0][i] + Fy * k.c[1][i] + Fz * k.c[2][i];
         return dot * k.invc[i] / absF;
     }
-    // collisionOperators.cuh:60-80
+    // collisionOperators.cuh:60-80.  With a density ratio the rest-state equilibrium of a
+    // moving direction is w_i (rho + K) (extension), so the recolouring uses that weight.
     R recolor(int i, R rr, R rb, R Fx, R Fy, R Fz, R absF) const {
         if (i == 0) return 0;
         const R rho = rr + rb;
         const R cos_i = cosphi(i, Fx, Fy, Fz, absF);
         const R coeff = k.beta * (rr * rb) / (rho * rho);
-        const R fieq = k.w[i] * rho;
+        const R fieq = k.ratio ? k.w[i] * (rho + rr * k.kappa_r + rb * k.kappa_b) : k.w[i] * rho;
         return coeff * cos_i * fieq;
     }
 

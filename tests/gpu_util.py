@@ -41,6 +41,30 @@ def field_errors(got: np.ndarray, ref: np.ndarray, idx=None):
     return [ol.rel_l2(got[f], ref[f]) for f in range(11)]
 
 
+GROUPS = {"rhor": [0], "rhob": [1], "u": [2, 3, 4], "Pi": [5, 6, 7, 8, 9, 10]}
+
+
+def group_errors(got: np.ndarray, ref: np.ndarray, idx=None) -> dict:
+    """Relative L2 error per moment group: each colour density, the velocity vector field
+    and the non-equilibrium stress tensor field (components pooled, so a component that is
+    identically zero in the reference does not make the metric ill-conditioned)."""
+    if idx is not None:
+        got, ref = got[idx], ref[idx]
+    return {k: ol.rel_l2(got[v], ref[v]) for k, v in GROUPS.items()}
+
+
+def assert_fp32_parity(got: np.ndarray, ref64: np.ndarray, ref32: np.ndarray, idx, gate: float = 1e-5,
+                       slack: float = 3.0, what: str = ""):
+    """The CUDA result must be within `gate` relative L2 of the FP64 oracle, or at least as
+    close to it as the reference's FP32 arithmetic is (times `slack`), for every group."""
+    eg = group_errors(got, ref64, idx)
+    er = group_errors(ref32, ref64, idx)
+    for k in GROUPS:
+        lim = max(gate, slack * er[k])
+        assert eg[k] <= lim, f"{what} {k}: gpu-vs-fp64 {eg[k]:.3e} > {lim:.3e} (fp32-vs-fp64 {er[k]:.3e})"
+    return eg, er
+
+
 def gpu_run(p: mbcg.Params, state: np.ndarray, nsteps: int, env=None) -> np.ndarray:
     old = {}
     for k, v in (env or {}).items():

@@ -1,7 +1,9 @@
 """CUDA library vs the reference's own outputs (golden fixtures) and vs the FP64 oracle.
 
-Tolerance: relative L2 per moment field <= 1e-5 after 100 steps in FP32 (the accuracy gate
-of the drop-in form); single steps from random states are held to 2e-6.
+Tolerance (relative L2, per colour density, velocity vector field and stress tensor field):
+1e-5 after 100 steps (2e-6 after one step), or, where the reference's own FP32 arithmetic
+already differs from the FP64 oracle by more than that (velocity and stress fields that are
+close to zero early in a run), at most 3x the reference-FP32-vs-FP64 difference.
 """
 import os
 
@@ -10,49 +12,58 @@ import pytest
 
 import mbcg
 import oracle_lib as ol
-from gpu_util import field_errors, gpu_from_ic, gpu_run, load_fixture, written_nodes
+from gpu_util import (assert_fp32_parity, field_errors, gpu_from_ic, gpu_run, group_errors, load_fixture,
+                      written_nodes)
 
 pytestmark = pytest.mark.gpu
-TOL_100 = 1e-5
-TOL_1 = 2e-6
+TOL = 1e-5      # relative L2 gate after 100 steps
+TOL_1 = 2e-6    # one step
 
 
 @pytest.mark.parametrize("q", [27, 19])
 def test_reference_jet_fixture(q):
+    """The reference's own jet (FP32, its initial condition) at steps 1, 10 and 100."""
     p, z = load_fixture(f"ref_jet_q{q}")
     idx = written_nodes(p)
+    o64 = z["init"].astype(np.float64)
     with mbcg.Case(p) as c:
         c.copy_in(z["init"])
         done = 0
         for n in (1, 10, 100):
             c.step(n - done)
+            o64 = ol.oracle_run(p, o64, n - done, first_step=done + 1)
             done = n
-            errs = field_errors(c.copy_out(), z[f"step{n}"], idx)
-            assert max(errs) < (TOL_1 if n == 1 else TOL_100), (n, errs)
+            got = c.copy_out()
+            assert_fp32_parity(got, o64, z[f"step{n}"], idx, what=f"q{q} step {n}")
+            # and directly against the reference's FP32 output
+            eg = group_errors(got, z[f"step{n}"], idx)
+            assert eg["rhor"] < TOL and eg["rhob"] < TOL, eg
 
 
 def test_reference_defaults_fixture():
+    """The reference exactly as shipped (tau = 1, sigma = 0.1, beta = 0.9), 20 steps."""
     p, z = load_fixture("ref_defaults_q27")
     got = gpu_run(p, z["init"], 20)
-    errs = field_errors(got, z["step20"], written_nodes(p))
-    assert max(errs) < TOL_100, errs
+    o64 = ol.oracle_run(p, z["init"].astype(np.float64), 20)
+    assert_fp32_parity(got, o64, z["step20"], written_nodes(p), what="defaults")
 
 
 @pytest.mark.parametrize("q", [27, 19])
 def test_reference_random_state_fixture(q):
+    """One step from a state where every node is an interface node (all terms active)."""
     p, z = load_fixture(f"ref_random_q{q}")
-    idx = written_nodes(p)
+    a = z["in_float"]
+    fl = (slice(None), slice(1, -1), slice(1, -1), slice(1, -1))
     with mbcg.Case(p) as c:
-        c.copy_in(z["in_float"])
+        c.copy_in(a)
         c.rcs()
         c.swap()
         got = c.copy_out()
-    fl = (slice(None), slice(1, -1), slice(1, -1), slice(1, -1))
-    errs = field_errors(got, z["rcs_float"], fl)
-    assert max(errs) < TOL_1, errs
-    got = gpu_run(p, z["in_float"], 1)
-    errs = field_errors(got, z["out_float"], idx)
-    assert max(errs) < TOL_1, errs
+    o64 = ol.oracle_step(p, a.astype(np.float64), 1, do_bc=False)
+    assert_fp32_parity(got, o64, z["rcs_float"], fl, gate=TOL_1, what=f"rcs q{q}")
+    got = gpu_run(p, a, 1)
+    o64 = ol.oracle_step(p, a.astype(np.float64), 1)
+    assert_fp32_parity(got, o64, z["out_float"], written_nodes(p), gate=TOL_1, what=f"step q{q}")
 
 
 def test_initial_conditions_match_oracle():
@@ -63,8 +74,8 @@ def test_initial_conditions_match_oracle():
             got = c.copy_out()
         ref = ol.oracle_init(p, np.float64)
         idx = written_nodes(p) if p.ic == mbcg.IC_JET else (slice(None),) + (slice(1, -1),) * 3
-        errs = field_errors(got, ref, idx)
-        assert max(errs[:5]) < 1e-6, (p.ic, errs)
+        eg = group_errors(got, ref, idx)
+        assert eg["rhor"] < 1e-6 and eg["rhob"] < 1e-6 and eg["u"] < 1e-6, (p.ic, eg)
 
 
 CASES = {
@@ -79,18 +90,14 @@ CASES = {
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_cases_vs_fp64_oracle(name):
+    """Cases beyond the reference's reach (fully periodic bubble, walls, gravity, density
+    ratio, z jet with noise and zero-gradient outflow) against the FP64 oracle, 100 steps."""
     p = CASES[name]()
     a = ol.oracle_init(p, np.float64)
-    ref = ol.oracle_run(p, a.copy(), 100)
+    o64 = ol.oracle_run(p, a.copy(), 100)
+    o32 = ol.oracle_run(p, a.astype(np.float32), 100)
     got = gpu_run(p, a, 100)
-    errs = field_errors(got, ref, written_nodes(p))
-    # velocity and stress fields of a flow at rest start at zero: judge them by the
-    # norm of the density-scaled reference instead when the reference is tiny
-    assert max(errs[:2]) < TOL_100, (name, errs)
-    for f in range(2, 11):
-        nref = np.linalg.norm(ref[written_nodes(p)][f])
-        if nref > 1e-9:
-            assert errs[f] < max(TOL_100, 1e-12 / nref * 1e6), (name, f, errs[f])
+    assert_fp32_parity(got, o64, o32, written_nodes(p), what=name)
 
 
 @pytest.mark.parametrize("axis", [0, 1, 2])
@@ -104,10 +111,10 @@ def test_inout_axis_generality(axis):
     p.jet_center[0] = (dims[others[0]] - 1) / 2.0
     p.jet_center[1] = (dims[others[1]] - 1) / 2.0
     a0 = ol.oracle_init(p, np.float64)
-    ref = ol.oracle_run(p, a0.copy(), 60)
+    o64 = ol.oracle_run(p, a0.copy(), 60)
+    o32 = ol.oracle_run(p, a0.astype(np.float32), 60)
     got = gpu_run(p, a0, 60)
-    errs = field_errors(got, ref, written_nodes(p))
-    assert max(errs[:5]) < TOL_100, (axis, errs)
+    assert_fp32_parity(got, o64, o32, written_nodes(p), what=f"inout axis {axis}")
 
 
 @pytest.mark.parametrize("axis", [0, 1])
@@ -123,10 +130,10 @@ def test_wall_axis_generality(axis):
     p.gravity[axis] = -1e-4
     p.rti_position = dims[axis] / 2.0
     a0 = ol.oracle_init(p, np.float64)
-    ref = ol.oracle_run(p, a0.copy(), 60)
+    o64 = ol.oracle_run(p, a0.copy(), 60)
+    o32 = ol.oracle_run(p, a0.astype(np.float32), 60)
     got = gpu_run(p, a0, 60)
-    errs = field_errors(got, ref, written_nodes(p))
-    assert max(errs[:2]) < TOL_100, (axis, errs)
+    assert_fp32_parity(got, o64, o32, written_nodes(p), what=f"wall axis {axis}")
 
 
 def test_tma_and_plain_load_paths_agree():
