@@ -47,7 +47,7 @@ constexpr int kTX = 30;    // destination columns per CTA
 constexpr int kRBX = 48;   // staged width of rhor/rhob rows (34 needed + 16-byte alignment slack)
 constexpr int kMX = 40;    // staged width of the other 9 fields (32 needed + slack)
 constexpr int kPSX = 34;   // psi ring width (32 sources + 1 on each side)
-constexpr int kNSTAGE = 4; // planes in flight: k-1, k, k+1, k+2
+constexpr int kNSTAGE = 3; // planes staged: k, k+1 and the one in flight, k+2
 constexpr unsigned kFull = 0xffffffffu;
 
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
@@ -291,13 +291,26 @@ __device__ __forceinline__ void add_pop(Acc& a, float g, float r, int ex, int ey
 }
 
 // ------------------------------------------------------------------ the kernel
+// fast reciprocal (MUFU-based, <= 2 ulp); the colour fraction of a pure node stays exact
+__device__ __forceinline__ float fast_rcp(float v) { return __fdividef(1.0f, v); }
+
+template <typename S>
+__device__ __forceinline__ void finalize_store(const StepParams& P, long long o, float rr, float rb, float ux,
+                                               float uy, float uz, const float (&pi)[6]) {
+    const float u[3] = {ux, uy, uz};
+    S out[NF];
+    encode<S>(P, rr, rb, u, pi, out);
+    store_node<S>(P, o, out);
+}
+
 template <int Q, typename S, int W, bool kTMA>
-__global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__ StepParams P,
+__global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__ StepParams P,
                                                          const __grid_constant__ TensorMaps T) {
     using G = Geo<S, W>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // TMA destinations need 128-byte alignment: round the dynamic base up (G::smem has slack)
-    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     float* psi_ring = reinterpret_cast<float*>(smem + G::off_psi);
     float* xbuf = reinterpret_cast<float*>(smem + G::off_xbuf);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G::off_bar);
@@ -307,8 +320,8 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
     const int tid = w * 32 + lane;
     const int nx = P.nx, ny = P.ny, nz = P.nz;
 
-    const int xb = kTX * blockIdx.x;      // source column of lane 0
-    const int yb = (W - 2) * blockIdx.y;  // source row of warp 0
+    const int xb = kTX * blockIdx.x;     // source column of lane 0
+    const int yb = (W - 2) * blockIdx.y; // source row of warp 0
     const int xs = xb + lane, ys = yb + w;
     const int zd0 = 1 + P.zchunk * blockIdx.z;
     const int zd1 = min(zd0 + P.zchunk, nz - 1);
@@ -316,18 +329,38 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
 
     const int xr0 = floor8(xb - 1); // first staged column of rhor/rhob
     const int xm0 = floor8(xb);     // first staged column of the other fields
-    const int offRB = xb - xr0;     // box column of lane 0 (rhor/rhob)
-    const int offM = xb - xm0;      // box column of lane 0 (other fields)
+    const int offRB = xb - xr0;
+    const int offM = xb - xm0;
+    const int bR = (w + 1) * kRBX + lane + offRB; // this node in the rhor/rhob boxes
+    const int bM = w * kMX + lane + offM;         // this node in the other boxes
 
     const bool dest_thread = lane >= 1 && lane <= kTX && w >= 1 && w <= W - 2 && xs <= nx - 2 && ys <= ny - 2;
-
-    // roles of this thread's column along x and y
     const int rx = axis_role(P, 0, xs, nx);
     const int ry = axis_role(P, 1, ys, ny);
-    const int mxs = data_coord(P, 0, xs, nx), mys = data_coord(P, 1, ys, ny);
     const bool col_in_box = (rx != R_IMAGE && ry != R_IMAGE);
+    const long long gxy = static_cast<long long>(data_coord(P, 1, ys, ny)) * P.pitch + data_coord(P, 0, xs, nx);
+    const int ia = P.inout_axis;
 
-    auto stage_ptr = [&](int k) -> unsigned char* { return smem + ((k - kfirst) & (kNSTAGE - 1)) * G::stage; };
+    // psi fill: each thread owns <= kPsiPer ring elements; their mapping never changes along z
+    constexpr int kPsiPer = (G::psi_plane + 32 * W - 1) / (32 * W);
+    int psi_box[kPsiPer];
+    long long psi_g[kPsiPer];
+#pragma unroll
+    for (int j = 0; j < kPsiPer; ++j) {
+        const int e = tid + j * 32 * W;
+        psi_box[j] = -2;
+        psi_g[j] = 0;
+        if (e < G::psi_plane) {
+            const int r = e / kPSX, c = e % kPSX;
+            const int gx = xb - 1 + c, gy = yb - 1 + r;
+            const int mx = psi_coord(P, 0, gx, nx), my = psi_coord(P, 1, gy, ny);
+            psi_box[j] = (mx == gx && my == gy) ? r * kRBX + c + offRB - 1 : -1;
+            psi_g[j] = static_cast<long long>(my) * P.pitch + mx;
+        }
+    }
+
+    auto slot_of = [&](int k) -> int { return (k - kfirst) % kNSTAGE; };
+    auto stage_ptr = [&](int k) -> unsigned char* { return smem + slot_of(k) * G::stage; };
     auto rb_box = [&](unsigned char* st, int f) -> S* { return reinterpret_cast<S*>(st + f * G::rb_field); };
     auto m_box = [&](unsigned char* st, int f) -> S* {
         return reinterpret_cast<S*>(st + 2 * G::rb_field + (f - 2) * G::m_field);
@@ -340,7 +373,7 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
         const int kz = zload(k);
         if constexpr (kTMA) {
             if (tid == 0) {
-                uint64_t* bar = &bars[(k - kfirst) & (kNSTAGE - 1)];
+                uint64_t* bar = &bars[slot_of(k)];
                 fence_proxy_async();
                 mbar_expect_tx(bar, G::tx);
                 tma_load_3d(rb_box(st, 0), &T.m[0], xr0, yb - 1, kz, bar);
@@ -373,7 +406,7 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
     auto wait_stage = [&](int k) -> bool {
         if constexpr (kTMA) {
             const int j = k - kfirst;
-            return mbar_wait_bounded(&bars[j & (kNSTAGE - 1)], static_cast<uint32_t>((j / kNSTAGE) & 1), kWaitLimit);
+            return mbar_wait_bounded(&bars[j % kNSTAGE], static_cast<uint32_t>((j / kNSTAGE) & 1), kWaitLimit);
         } else {
             return true;
         }
@@ -384,34 +417,32 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
         if constexpr (kTMA) {
             for (int k = k_failed + 1; k <= k_issued; ++k) {
                 const int j = k - kfirst;
-                mbar_wait_bounded(&bars[j & (kNSTAGE - 1)], static_cast<uint32_t>((j / kNSTAGE) & 1), kWaitLimit / 4);
+                mbar_wait_bounded(&bars[j % kNSTAGE], static_cast<uint32_t>((j / kNSTAGE) & 1), kWaitLimit / 4);
             }
         }
     };
 
-    // ---- psi ring ----------------------------------------------------------------
-    // psi (utilities/mathUtilities.cuh:12-19) of plane k at columns xb-1..xb+32 and rows
-    // yb-1..yb+W, with the colour-gradient neighbour rule applied to every coordinate.
+    // ---- psi ring: psi = (rhor - rhob)/rho (mathUtilities.cuh:12-19) of plane k over
+    // columns xb-1..xb+32 and rows yb-1..yb+W, colour-gradient neighbour rule applied
     auto fill_psi = [&](int k) {
         float* ring = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
         const int mz = psi_coord(P, 2, k, nz);
-        const int kz = zload(k);
+        const bool plane_in_box = (mz == zload(k));
+        const long long zo = static_cast<long long>(mz) * P.plane;
         unsigned char* st = stage_ptr(k);
         const S* r0b = rb_box(st, 0);
         const S* r1b = rb_box(st, 1);
-        for (int e = tid; e < G::psi_plane; e += 32 * W) {
-            const int r = e / kPSX, c = e % kPSX;
-            const int gx = xb - 1 + c, gy = yb - 1 + r;
-            const int mx = psi_coord(P, 0, gx, nx), my = psi_coord(P, 1, gy, ny);
+#pragma unroll
+        for (int j = 0; j < kPsiPer; ++j) {
+            if (psi_box[j] == -2) continue;
             float v;
-            if (mx == gx && my == gy && mz == kz) {
-                const int bi = r * kRBX + c + offRB - 1;
-                v = psi_of<S>(P, r0b[bi], r1b[bi]);
+            if (plane_in_box && psi_box[j] >= 0) {
+                v = psi_of<S>(P, r0b[psi_box[j]], r1b[psi_box[j]]);
             } else {
-                const long long o = static_cast<long long>(mz) * P.plane + static_cast<long long>(my) * P.pitch + mx;
+                const long long o = zo + psi_g[j];
                 v = psi_of<S>(P, static_cast<const S*>(P.a[0])[o], static_cast<const S*>(P.a[1])[o]);
             }
-            ring[e] = v;
+            ring[tid + j * 32 * W] = v;
         }
     };
 
@@ -423,11 +454,11 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
         }
         __syncthreads();
     }
-    int k_issued = kfirst + 2;
+    int k_issued = kfirst + kNSTAGE - 1;
     for (int k = kfirst; k <= k_issued; ++k) issue(k);
     if constexpr (!kTMA) __syncthreads();
     {
-        bool ok = wait_stage(kfirst) && wait_stage(kfirst + 1);
+        const bool ok = wait_stage(kfirst) && wait_stage(kfirst + 1);
         if (__syncthreads_or(!ok)) {
             bail(kfirst - 1, k_issued);
             return;
@@ -443,18 +474,21 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
 
     constexpr float w0 = Stencil<Q>::wk(0);
     constexpr float cs2 = 1.0f / 3.0f;
+    float* xb_self = xbuf + w * 32 + lane;
 
     for (int k = zd0 - 1; k <= zd1; ++k) {
         // (1) psi of plane k+1
-        const bool ok = wait_stage(k + 1);
-        if (__syncthreads_or(!ok)) {
-            bail(k, k_issued);
-            return;
+        {
+            const bool ok = wait_stage(k + 1);
+            if (__syncthreads_or(!ok)) {
+                bail(k, k_issued);
+                return;
+            }
         }
         fill_psi(k + 1);
         __syncthreads();
-        // (2) prefetch plane k+2 into the slot plane k-2 used
-        if (k + 2 <= zd1 + 1) {
+        // (2) prefetch plane k+2 into the slot plane k-1 used
+        if (k + 2 <= zd1 + 1 && k + 2 > k_issued) {
             issue(k + 2);
             k_issued = k + 2;
         }
@@ -465,149 +499,157 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
         if (rx == R_OUT || ry == R_OUT || rz == R_OUT) role = R_OUT;
         else if (rx == R_WALL || ry == R_WALL || rz == R_WALL) role = R_WALL;
         else if (rx == R_GHOST || ry == R_GHOST || rz == R_GHOST) role = R_GHOST;
+        const bool active = (role == R_FLUID || role == R_GHOST);
 
         unsigned char* st = stage_ptr(k);
         const int kz = zload(k);
+        const long long kzo = static_cast<long long>(kz) * P.plane;
         Node<S> nd{};
-        Node<S> fn{}; // first-fluid node of a ghost source
-        if (role == R_FLUID || role == R_GHOST) {
+        Node<S> fn{}; // first-fluid node of a ghost source (lbm.cuh:85-89)
+        if (active) {
             float v[NF];
             if (col_in_box) {
-                const int bR = (w + 1) * kRBX + lane + offRB;
-                const int bM = w * kMX + lane + offM;
                 v[0] = Codec<S>::to_f(rb_box(st, 0)[bR]);
                 v[1] = Codec<S>::to_f(rb_box(st, 1)[bR]);
 #pragma unroll
                 for (int f = 2; f < NF; ++f) v[f] = Codec<S>::to_f(m_box(st, f)[bM]);
             } else {
-                load_global<S>(P, static_cast<long long>(kz) * P.plane + static_cast<long long>(mys) * P.pitch + mxs, v);
+                load_global<S>(P, kzo + gxy, v);
             }
             decode<S>(P, v, nd);
             if (role == R_GHOST) {
-                // neighbour along the inlet/outlet axis into the domain (lbm.cuh:85-89)
-                int fx = xs, fy = ys, fk = k;
-                if (rx == R_GHOST) fx = (xs == 0) ? 1 : nx - 2;
-                if (ry == R_GHOST) fy = (ys == 0) ? 1 : ny - 2;
-                if (rz == R_GHOST) fk = (k == 0) ? 1 : nz - 2;
                 float u[NF];
-                if (col_in_box) {
-                    unsigned char* sf = stage_ptr(fk);
-                    const int bM = (w + (fy - ys)) * kMX + lane + (fx - xs) + offM;
+                if (rz == R_GHOST) {
+                    // z inlet/outlet ghost: first fluid plane 1 (staged) or nz-2 (global)
+                    if (k == 0 && col_in_box) {
+                        unsigned char* sf = stage_ptr(k + 1);
 #pragma unroll
-                    for (int f = 2; f < NF; ++f) u[f] = Codec<S>::to_f(m_box(sf, f)[bM]);
+                        for (int f = 2; f < NF; ++f) u[f] = Codec<S>::to_f(m_box(sf, f)[bM]);
+                        u[0] = u[1] = 1.0f;
+                    } else {
+                        load_global<S>(P, static_cast<long long>(k == 0 ? 1 : nz - 2) * P.plane + gxy, u);
+                    }
+                } else if (col_in_box) {
+                    const int dx = (rx == R_GHOST) ? (xs == 0 ? 1 : -1) : 0;
+                    const int dy = (ry == R_GHOST) ? (ys == 0 ? 1 : -1) : 0;
+                    const int b2 = bM + dy * kMX + dx;
+#pragma unroll
+                    for (int f = 2; f < NF; ++f) u[f] = Codec<S>::to_f(m_box(st, f)[b2]);
                     u[0] = u[1] = 1.0f;
                 } else {
+                    const int fx = (rx == R_GHOST) ? (xs == 0 ? 1 : nx - 2) : xs;
+                    const int fy = (ry == R_GHOST) ? (ys == 0 ? 1 : ny - 2) : ys;
                     load_global<S>(P,
-                                   static_cast<long long>(zload(fk)) * P.plane +
-                                       static_cast<long long>(data_coord(P, 1, fy, ny)) * P.pitch + data_coord(P, 0, fx, nx),
+                                   kzo + static_cast<long long>(data_coord(P, 1, fy, ny)) * P.pitch +
+                                       data_coord(P, 0, fx, nx),
                                    u);
                 }
                 decode<S>(P, u, fn);
             }
         }
 
-        // coefficient tensor and colour split
+        // coefficient tensor and colour split; inactive sources keep all-zero coefficients
         Coef cf{};
         float aR = 0.0f, dcoef = 0.0f, Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
         bool iface = false;
-        if (role == R_FLUID) {
+        if (active) {
             const float rho = nd.rr + nd.rb;
-            aR = __fdiv_rn(nd.rr, rho);
-            const float inv = __fdiv_rn(1.0f, rho);
-            iface = (4.0f * nd.rr * nd.rb * inv * inv) > 1.0e-4f; // lbm.cuh:181,187
-            build_coef(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, nd.ux, nd.uy, nd.uz, nd.pxx, nd.pxy, nd.pyy,
-                       nd.pyz, nd.pzz, nd.pxz);
-        } else if (role == R_GHOST) {
-            const float rho = nd.rr + nd.rb;
-            aR = __fdiv_rn(nd.rr, rho);
-            build_coef(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, fn.ux, fn.uy, fn.uz, fn.pxx, fn.pxy, fn.pyy,
-                       fn.pyz, fn.pzz, fn.pxz);
+            const float inv = fast_rcp(rho);
+            aR = nd.rb == 0.0f ? 1.0f : (nd.rr == 0.0f ? 0.0f : nd.rr * inv);
+            if (role == R_FLUID) {
+                iface = (4.0f * nd.rr * nd.rb * inv * inv) > 1.0e-4f; // lbm.cuh:181,187
+                build_coef(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, nd.ux, nd.uy, nd.uz, nd.pxx, nd.pxy,
+                           nd.pyy, nd.pyz, nd.pzz, nd.pxz);
+            } else {
+                build_coef(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, fn.ux, fn.uy, fn.uz, fn.pxx, fn.pxy,
+                           fn.pyy, fn.pyz, fn.pzz, fn.pxz);
+            }
         }
-        if (__any_sync(kFull, iface)) {
-            if (iface) {
-                // colour gradient at the source (forces.cuh:20-60) from the psi ring
-                const float* rm = psi_ring + ((k - 1 - kfirst) % 3) * G::psi_plane;
-                const float* r0p = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
-                const float* rp = psi_ring + ((k + 1 - kfirst) % 3) * G::psi_plane;
-                float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        const bool any_iface = __any_sync(kFull, iface);
+        if (any_iface && iface) {
+            // colour gradient at the source (forces.cuh:20-60) from the psi ring
+            const float* rm = psi_ring + ((k - 1 - kfirst) % 3) * G::psi_plane;
+            const float* r0p = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
+            const float* rp = psi_ring + ((k + 1 - kfirst) % 3) * G::psi_plane;
+            float sx = 0.0f, sy = 0.0f, sz = 0.0f;
 #pragma unroll
-                for (int dz = -1; dz <= 1; ++dz) {
-                    const float* ring = dz < 0 ? rm : (dz == 0 ? r0p : rp);
+            for (int dz = -1; dz <= 1; ++dz) {
+                const float* ring = dz < 0 ? rm : (dz == 0 ? r0p : rp);
 #pragma unroll
-                    for (int dy = -1; dy <= 1; ++dy) {
+                for (int dy = -1; dy <= 1; ++dy) {
 #pragma unroll
-                        for (int dx = -1; dx <= 1; ++dx) {
-                            constexpr int dummy = 0;
-                            (void)dummy;
-                            if (dx == 0 && dy == 0 && dz == 0) continue;
-                            if (!Stencil<Q>::has(dx, dy, dz)) continue;
-                            const float ps = ring[(w + 1 + dy) * kPSX + lane + 1 + dx];
-                            const float wp = weight<Q>(dx, dy, dz) * ps;
-                            if (dx) sx += dx * wp;
-                            if (dy) sy += dy * wp;
-                            if (dz) sz += dz * wp;
-                        }
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        if (dx == 0 && dy == 0 && dz == 0) continue;
+                        if (!Stencil<Q>::has(dx, dy, dz)) continue;
+                        const float ps = ring[(w + 1 + dy) * kPSX + lane + 1 + dx];
+                        const float wp = weight<Q>(dx, dy, dz) * ps;
+                        if (dx) sx += dx * wp;
+                        if (dy) sy += dy * wp;
+                        if (dz) sz += dz * wp;
                     }
                 }
-                Fx = 3.0f * sx;
-                Fy = 3.0f * sy;
-                Fz = 3.0f * sz;
-                const float absF = sqrtf(Fx * Fx + Fy * Fy + Fz * Fz);
-                // Omega2 (collisionOperators.cuh:16-25) folded into the coefficients
-                const float hA = 0.5f * P.A * absF;
-                cf.p000 -= hA;
-                cf.r0 -= hA * (Stencil<Q>::B0 - w0);
-                if (absF > 1.0e-4f) {
-                    const float qf = 0.5f * P.A / absF;
-                    cf.p200 += qf * Fx * Fx;
-                    cf.p020 += qf * Fy * Fy;
-                    cf.p002 += qf * Fz * Fz;
-                    cf.p110 += 2.0f * qf * Fx * Fy;
-                    cf.p101 += 2.0f * qf * Fx * Fz;
-                    cf.p011 += 2.0f * qf * Fy * Fz;
-                    // recolouring (collisionOperators.cuh:60-80): beta rr rb / (rho |F|); with a
-                    // density ratio the rest equilibrium of moving directions is w (rho + K)
-                    const float rho = nd.rr + nd.rb;
-                    const float feq0 = P.ratio ? rho + nd.rr * P.kappa_r + nd.rb * P.kappa_b : rho;
-                    dcoef = P.beta * (nd.rr * nd.rb) / (rho * rho * absF) * feq0;
-                }
+            }
+            Fx = 3.0f * sx;
+            Fy = 3.0f * sy;
+            Fz = 3.0f * sz;
+            const float absF = sqrtf(Fx * Fx + Fy * Fy + Fz * Fz);
+            // Omega2 (collisionOperators.cuh:16-25) folded into the coefficients
+            const float hA = 0.5f * P.A * absF;
+            cf.p000 -= hA;
+            cf.r0 -= hA * (Stencil<Q>::B0 - w0);
+            if (absF > 1.0e-4f) {
+                const float ia_ = fast_rcp(absF);
+                const float qf = 0.5f * P.A * ia_;
+                cf.p200 += qf * Fx * Fx;
+                cf.p020 += qf * Fy * Fy;
+                cf.p002 += qf * Fz * Fz;
+                cf.p110 += 2.0f * qf * Fx * Fy;
+                cf.p101 += 2.0f * qf * Fx * Fz;
+                cf.p011 += 2.0f * qf * Fy * Fz;
+                // recolouring (collisionOperators.cuh:60-80): beta rr rb / (rho^2 |F|) * feq0, where
+                // the rest equilibrium of moving directions is w rho (w (rho + K) with a density ratio)
+                const float rho = nd.rr + nd.rb;
+                const float feq0 = P.ratio ? rho + nd.rr * P.kappa_r + nd.rb * P.kappa_b : rho;
+                const float irho = fast_rcp(rho);
+                dcoef = P.beta * (nd.rr * nd.rb) * irho * irho * ia_ * feq0;
             }
         }
 
-        // separable inverse transform: x-pass t_bc(cx), y-pass s_c(cx, cy)
-        float s0[3][3], s1[3][3], s2[3][3];
+        // separable inverse transform: x-pass t_bc(cx), y-pass s_c(cx, cy); e = s0 + s2
+        float s0[3][3], s1[3][3], e2[3][3];
         {
             float t00[3], t10[3], t01[3], t20[3], t02[3], t11[3];
-            {
-                const float a = cf.p000 + cf.p200;
-                t00[1] = cf.p000; t00[2] = a + cf.p100; t00[0] = a - cf.p100;
-                const float b = cf.p010 + cf.p210;
-                t10[1] = cf.p010; t10[2] = b + cf.p110; t10[0] = b - cf.p110;
-                const float d = cf.p001 + cf.p201;
-                t01[1] = cf.p001; t01[2] = d + cf.p101; t01[0] = d - cf.p101;
-                t20[1] = cf.p020; t20[2] = cf.p020 + cf.p120; t20[0] = cf.p020 - cf.p120;
-                t02[1] = cf.p002; t02[2] = cf.p002 + cf.p102; t02[0] = cf.p002 - cf.p102;
-                t11[1] = cf.p011; t11[2] = cf.p011 + cf.p111; t11[0] = cf.p011 - cf.p111;
-            }
+            const float a = cf.p000 + cf.p200;
+            t00[1] = cf.p000; t00[2] = a + cf.p100; t00[0] = a - cf.p100;
+            const float b = cf.p010 + cf.p210;
+            t10[1] = cf.p010; t10[2] = b + cf.p110; t10[0] = b - cf.p110;
+            const float d = cf.p001 + cf.p201;
+            t01[1] = cf.p001; t01[2] = d + cf.p101; t01[0] = d - cf.p101;
+            t20[1] = cf.p020; t20[2] = cf.p020 + cf.p120; t20[0] = cf.p020 - cf.p120;
+            t02[1] = cf.p002; t02[2] = cf.p002 + cf.p102; t02[0] = cf.p002 - cf.p102;
+            t11[1] = cf.p011; t11[2] = cf.p011 + cf.p111; t11[0] = cf.p011 - cf.p111;
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
                 const float e0 = t00[i] + t20[i];
                 s0[i][1] = t00[i]; s0[i][2] = e0 + t10[i]; s0[i][0] = e0 - t10[i];
                 const float e1 = t01[i] + cf.p021;
                 s1[i][1] = t01[i]; s1[i][2] = e1 + t11[i]; s1[i][0] = e1 - t11[i];
-                s2[i][1] = t02[i]; s2[i][2] = t02[i] + cf.p012; s2[i][0] = t02[i] - cf.p012;
+                e2[i][1] = s0[i][1] + t02[i];
+                e2[i][2] = s0[i][2] + (t02[i] + cf.p012);
+                e2[i][0] = s0[i][0] + (t02[i] - cf.p012);
             }
         }
-        // recolouring strengths per shell, d_s = dcoef * w_s / |c|
+        // recolouring strength per shell, d_s = dcoef * w_s / |c|
         const float dk1 = dcoef * weight<Q>(1, 0, 0);
         const float dk2 = dcoef * weight<Q>(1, 1, 0) * 0.7071067811865475f;
         const float dk3 = dcoef * weight<Q>(1, 1, 1) * 0.5773502691896258f;
 
         // wall bounce-back of this node's own populations (destination = this node, plane k)
-        const bool wall_x0 = P.bc[0] == MBCG_BC_WALL && xs == 1, wall_x1 = P.bc[0] == MBCG_BC_WALL && xs == nx - 2;
-        const bool wall_y0 = P.bc[1] == MBCG_BC_WALL && ys == 1, wall_y1 = P.bc[1] == MBCG_BC_WALL && ys == ny - 2;
-        const bool wall_z0 = P.bc[2] == MBCG_BC_WALL && k == 1, wall_z1 = P.bc[2] == MBCG_BC_WALL && k == nz - 2;
-        const bool reflect = role == R_FLUID && dest_thread && (wall_x0 | wall_x1 | wall_y0 | wall_y1 | wall_z0 | wall_z1);
+        const bool wx0 = P.bc[0] == MBCG_BC_WALL && xs == 1, wx1 = P.bc[0] == MBCG_BC_WALL && xs == nx - 2;
+        const bool wy0 = P.bc[1] == MBCG_BC_WALL && ys == 1, wy1 = P.bc[1] == MBCG_BC_WALL && ys == ny - 2;
+        const bool wz0 = P.bc[2] == MBCG_BC_WALL && k == 1, wz1 = P.bc[2] == MBCG_BC_WALL && k == nz - 2;
+        const bool reflect = role == R_FLUID && dest_thread && (wx0 | wx1 | wy0 | wy1 | wz0 | wz1);
+        const bool any_reflect = __any_sync(kFull, reflect);
 
         // ---- per class cz: populations, x streaming, own-row moments, y exchange ----
         auto do_class = [&](auto czc, Acc& acc) {
@@ -618,30 +660,41 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     const int cx = i - 1, cy = j - 1;
-                    if (!Stencil<Q>::has(cx, cy, cz) || (role != R_FLUID && role != R_GHOST)) {
+                    if (!Stencil<Q>::has(cx, cy, cz)) {
                         g[i][j] = 0.0f;
-                        r[i][j] = 0.0f;
                         continue;
                     }
-                    float vv = cz == 0 ? s0[i][j] : (cz > 0 ? (s0[i][j] + s2[i][j]) + s1[i][j] : (s0[i][j] + s2[i][j]) - s1[i][j]);
+                    const float vv = cz == 0 ? s0[i][j] : (cz > 0 ? e2[i][j] + s1[i][j] : e2[i][j] - s1[i][j]);
                     float gi = weight<Q>(cx, cy, cz) * vv;
                     if (cx == 0 && cy == 0 && cz == 0) gi += cf.r0;
                     g[i][j] = gi;
-                    const int sh = cx * cx + cy * cy + cz * cz;
-                    const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
-                    const float delta = sh == 0 ? 0.0f : dks * (Fx * cx + Fy * cy + Fz * cz);
-                    r[i][j] = fmaf(aR, gi, delta);
                 }
             }
-            if (reflect) {
+            if (any_iface) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        const int cx = i - 1, cy = j - 1, sh = cx * cx + cy * cy + cz * cz;
+                        const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
+                        const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
+                        r[i][j] = sh == 0 ? aR * g[i][j] : fmaf(aR, g[i][j], dks * fc);
+                    }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) r[i][j] = aR * g[i][j];
+            }
+            if (any_reflect && reflect) {
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
                         const int cx = i - 1, cy = j - 1;
                         if (!Stencil<Q>::has(cx, cy, cz)) continue;
-                        const bool into = (wall_x0 && cx < 0) || (wall_x1 && cx > 0) || (wall_y0 && cy < 0) ||
-                                          (wall_y1 && cy > 0) || (wall_z0 && cz < 0) || (wall_z1 && cz > 0);
+                        const bool into = (wx0 && cx < 0) || (wx1 && cx > 0) || (wy0 && cy < 0) || (wy1 && cy > 0) ||
+                                          (wz0 && cz < 0) || (wz1 && cz > 0);
                         if (into) add_pop(accC, g[i][j], r[i][j], -cx, -cy, -cz);
                     }
             }
@@ -655,10 +708,10 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
                     const float gr = __shfl_down_sync(kFull, g[0][j], 1);
                     const float rl = __shfl_up_sync(kFull, r[2][j], 1);
                     const float rr_ = __shfl_down_sync(kFull, r[0][j], 1);
-                    X0[j] = gl + g[1][j] + gr;
-                    X1[j] = gl - gr;
                     X2[j] = gl + gr;
-                    XR[j] = rl + r[1][j] + rr_;
+                    X0[j] = X2[j] + g[1][j];
+                    X1[j] = gl - gr;
+                    XR[j] = (rl + rr_) + r[1][j];
                 } else {
                     X0[j] = g[1][j];
                     X1[j] = 0.0f;
@@ -678,8 +731,8 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
             }
             // cy = +1 goes to row w+1 (slot 0), cy = -1 to row w-1 (slot 1)
             constexpr int cls = cz + 1;
-            float* b0 = xbuf + ((cls * 2 + 0) * 4) * (W * 32) + w * 32 + lane;
-            float* b1 = xbuf + ((cls * 2 + 1) * 4) * (W * 32) + w * 32 + lane;
+            float* b0 = xb_self + ((cls * 2 + 0) * 4) * (W * 32);
+            float* b1 = xb_self + ((cls * 2 + 1) * 4) * (W * 32);
             b0[0 * W * 32] = X0[2];
             b0[1 * W * 32] = X1[2];
             b0[2 * W * 32] = X2[2];
@@ -698,27 +751,29 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
         auto gather = [&](auto czc, Acc& acc) {
             constexpr int cz = decltype(czc)::value;
             constexpr int cls = cz + 1;
-            if (w < 1 || w > W - 2) return;
-            const float* p0 = xbuf + ((cls * 2 + 0) * 4) * (W * 32) + (w - 1) * 32 + lane;
-            const float* m1 = xbuf + ((cls * 2 + 1) * 4) * (W * 32) + (w + 1) * 32 + lane;
+            const float* p0 = xb_self - 32 + ((cls * 2 + 0) * 4) * (W * 32);
+            const float* m1 = xb_self + 32 + ((cls * 2 + 1) * 4) * (W * 32);
             const float P0 = p0[0], P1 = p0[W * 32], P2 = p0[2 * W * 32], PR = p0[3 * W * 32];
             const float M0 = m1[0], M1 = m1[W * 32], M2 = m1[2 * W * 32], MR = m1[3 * W * 32];
             const float s00 = P0 + M0;
+            const float s10 = P1 + M1;
+            const float d00 = P0 - M0;
             acc.rho += s00;
-            acc.jx += P1 + M1;
+            acc.jx += s10;
             acc.xx += P2 + M2;
-            acc.jy += P0 - M0;
+            acc.jy += d00;
             acc.xy += P1 - M1;
             acc.yy += s00;
             acc.red += PR + MR;
             if (cz != 0) {
                 acc.jz += cz * s00;
-                acc.xz += cz * (P1 + M1);
-                acc.yz += cz * (P0 - M0);
+                acc.xz += cz * s10;
+                acc.yz += cz * d00;
                 acc.zz += s00;
             }
         };
-        gather(std::integral_constant<int, -1>{}, accP);
+        const bool dest_row = (w >= 1 && w <= W - 2);
+        if (dest_row) gather(std::integral_constant<int, -1>{}, accP);
 
         // (5) destination plane k-1 is complete: moments (lbm.cuh:239-261), store, boundary
         const int d = k - 1;
@@ -726,36 +781,31 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
             const float rho = accP.rho;
             const float rr = accP.red;
             const float rb = rho - rr;
-            const float inv = __fdiv_rn(1.0f, rho);
-            float Fb[3] = {0.0f, 0.0f, 0.0f};
-            float u[3];
+            const float inv = fast_rcp(rho);
+            float Fbx = 0.0f, Fby = 0.0f, Fbz = 0.0f;
             if (P.forced) {
-                Fb[0] = rho * P.g[0];
-                Fb[1] = rho * P.g[1];
-                Fb[2] = rho * P.g[2];
-                u[0] = (accP.jx + 0.5f * Fb[0]) * inv;
-                u[1] = (accP.jy + 0.5f * Fb[1]) * inv;
-                u[2] = (accP.jz + 0.5f * Fb[2]) * inv;
-            } else {
-                u[0] = accP.jx * inv;
-                u[1] = accP.jy * inv;
-                u[2] = accP.jz * inv;
+                Fbx = rho * P.g[0];
+                Fby = rho * P.g[1];
+                Fbz = rho * P.g[2];
             }
+            const float ux = (accP.jx + 0.5f * Fbx) * inv;
+            const float uy = (accP.jy + 0.5f * Fby) * inv;
+            const float uz = (accP.jz + 0.5f * Fbz) * inv;
             const float ctr = cs2 * rho;
             float pi[6];
-            pi[0] = (accP.xx - ctr) - rho * u[0] * u[0];
-            pi[1] = accP.xy - rho * u[0] * u[1];
-            pi[2] = (accP.yy - ctr) - rho * u[1] * u[1];
-            pi[3] = accP.yz - rho * u[1] * u[2];
-            pi[4] = (accP.zz - ctr) - rho * u[2] * u[2];
-            pi[5] = accP.xz - rho * u[0] * u[2];
+            pi[0] = (accP.xx - ctr) - rho * ux * ux;
+            pi[1] = accP.xy - rho * ux * uy;
+            pi[2] = (accP.yy - ctr) - rho * uy * uy;
+            pi[3] = accP.yz - rho * uy * uz;
+            pi[4] = (accP.zz - ctr) - rho * uz * uz;
+            pi[5] = accP.xz - rho * ux * uz;
             if (P.forced) {
-                pi[0] += u[0] * Fb[0];
-                pi[1] += 0.5f * (u[0] * Fb[1] + u[1] * Fb[0]);
-                pi[2] += u[1] * Fb[1];
-                pi[3] += 0.5f * (u[1] * Fb[2] + u[2] * Fb[1]);
-                pi[4] += u[2] * Fb[2];
-                pi[5] += 0.5f * (u[0] * Fb[2] + u[2] * Fb[0]);
+                pi[0] += ux * Fbx;
+                pi[1] += 0.5f * (ux * Fby + uy * Fbx);
+                pi[2] += uy * Fby;
+                pi[3] += 0.5f * (uy * Fbz + uz * Fby);
+                pi[4] += uz * Fbz;
+                pi[5] += 0.5f * (ux * Fbz + uz * Fbx);
             }
             if (P.ratio) {
                 const float Kc = (rr * P.kappa_r + rb * P.kappa_b) * cs2;
@@ -763,48 +813,49 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
                 pi[2] -= Kc;
                 pi[4] -= Kc;
             }
-            S out[NF];
-            encode<S>(P, rr, rb, u, pi, out);
             const long long o = static_cast<long long>(d) * P.plane + static_cast<long long>(ys) * P.pitch + xs;
-            store_node<S>(P, o, out);
+            finalize_store<S>(P, o, rr, rb, ux, uy, uz, pi);
 
-            if (P.do_bc && P.inout_axis >= 0) {
-                const int a = P.inout_axis;
-                const int pos[3] = {xs, ys, d};
-                const int n3[3] = {nx, ny, nz};
-                if (pos[a] == 1 || pos[a] == n3[a] - 2) {
-                    const bool inlet = pos[a] == 1;
-                    int gpos[3] = {xs, ys, d};
-                    gpos[a] = inlet ? 0 : n3[a] - 1;
-                    const long long og = static_cast<long long>(gpos[2]) * P.plane +
-                                         static_cast<long long>(gpos[1]) * P.pitch + gpos[0];
-                    S gv[NF];
+            if (P.do_bc && ia >= 0) {
+                // inlet / outlet functors fused into the first and last fluid layer
+                const int pa = ia == 0 ? xs : (ia == 1 ? ys : d);
+                const int na = ia == 0 ? nx : (ia == 1 ? ny : nz);
+                if (pa == 1 || pa == na - 2) {
+                    const bool inlet = pa == 1;
+                    const int gx = ia == 0 ? (inlet ? 0 : nx - 1) : xs;
+                    const int gy = ia == 1 ? (inlet ? 0 : ny - 1) : ys;
+                    const int gz = ia == 2 ? (inlet ? 0 : nz - 1) : d;
+                    const long long og = static_cast<long long>(gz) * P.plane + static_cast<long long>(gy) * P.pitch + gx;
+                    float orr, orb, oux, ouy, ouz;
                     if (inlet) {
                         // jet/boundary_conditions.cuh:16-39 (+ seeded per-node noise)
-                        const int t0 = a == 0 ? 1 : 0, t1 = a == 2 ? 1 : 2;
-                        const float du = static_cast<float>(pos[t0]) - P.jet_c0;
-                        const float dv = static_cast<float>(pos[t1]) - P.jet_c1;
+                        const int t0 = ia == 0 ? ys : xs;
+                        const int t1 = ia == 2 ? ys : d;
+                        const float du = static_cast<float>(t0) - P.jet_c0;
+                        const float dv = static_cast<float>(t1) - P.jet_c1;
                         const float m = (du * du + dv * dv) <= (P.jet_radius * P.jet_radius) ? 1.0f : 0.0f;
-                        const float grr = P.jet_blue ? (1.0f - m) * P.rho_r0 : m * P.rho_r0;
-                        const float grb = P.jet_blue ? m * P.rho_b0 : (1.0f - m) * P.rho_b0;
+                        orr = P.jet_blue ? (1.0f - m) * P.rho_r0 : m * P.rho_r0;
+                        orb = P.jet_blue ? m * P.rho_b0 : (1.0f - m) * P.rho_b0;
                         float gu[3] = {0.0f, 0.0f, 0.0f};
-                        gu[a] = m * P.jet_velocity;
-                        if (P.noise_amp != 0.0f && m != 0.0f) {
-                            const unsigned long long node = static_cast<unsigned long long>(gpos[0]) +
-                                                            static_cast<unsigned long long>(gpos[1]) * nx +
-                                                            static_cast<unsigned long long>(gpos[2]) * nx * ny;
-                            for (int cmp = 0; cmp < 3; ++cmp)
-                                gu[cmp] += m * P.noise_amp * noise_xi(P.seed, P.step, node, cmp);
+                        if (m != 0.0f) {
+                            if (P.noise_amp != 0.0f) {
+                                const unsigned long long node = static_cast<unsigned long long>(gx) +
+                                                                static_cast<unsigned long long>(gy) * nx +
+                                                                static_cast<unsigned long long>(gz) * nx * ny;
+                                gu[0] = m * P.noise_amp * noise_xi(P.seed, P.step, node, 0);
+                                gu[1] = m * P.noise_amp * noise_xi(P.seed, P.step, node, 1);
+                                gu[2] = m * P.noise_amp * noise_xi(P.seed, P.step, node, 2);
+                            }
                         }
-                        encode<S>(P, grr, grb, gu, pi, gv);
+                        oux = gu[0] + (ia == 0 ? m * P.jet_velocity : 0.0f);
+                        ouy = gu[1] + (ia == 1 ? m * P.jet_velocity : 0.0f);
+                        ouz = gu[2] + (ia == 2 ? m * P.jet_velocity : 0.0f);
                     } else if (P.outlet == MBCG_OUTLET_ZERO_GRADIENT) {
-#pragma unroll
-                        for (int f = 0; f < NF; ++f) gv[f] = out[f];
+                        orr = rr; orb = rb; oux = ux; ouy = uy; ouz = uz;
                     } else {
                         // convective outlet (jet/boundary_conditions.cuh:45-109), old ghost from A
                         float ov[NF];
-                        if (a == 2) {
-                            const int bR = (w + 1) * kRBX + lane + offRB, bM = w * kMX + lane + offM;
+                        if (ia == 2 && col_in_box) {
                             ov[0] = Codec<S>::to_f(rb_box(st, 0)[bR]);
                             ov[1] = Codec<S>::to_f(rb_box(st, 1)[bR]);
 #pragma unroll
@@ -814,25 +865,26 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
                         }
                         Node<S> on{};
                         decode<S>(P, ov, on);
-                        const float uc = fminf(fmaxf(u[a], 0.0f), 1.0f);
-                        float orr, orb, ou[3];
+                        const float ua = ia == 0 ? ux : (ia == 1 ? uy : uz);
+                        const float uc = fminf(fmaxf(ua, 0.0f), 1.0f);
                         if (on.rr + on.rb <= 1.0e-20f) {
-                            orr = rr; orb = rb; ou[0] = u[0]; ou[1] = u[1]; ou[2] = u[2];
+                            orr = rr; orb = rb; oux = ux; ouy = uy; ouz = uz;
                         } else {
                             orr = on.rr - uc * (on.rr - rr);
                             orb = on.rb - uc * (on.rb - rb);
-                            ou[0] = on.ux - uc * (on.ux - u[0]);
-                            ou[1] = on.uy - uc * (on.uy - u[1]);
-                            ou[2] = on.uz - uc * (on.uz - u[2]);
+                            oux = on.ux - uc * (on.ux - ux);
+                            ouy = on.uy - uc * (on.uy - uy);
+                            ouz = on.uz - uc * (on.uz - uz);
                         }
-                        encode<S>(P, orr, orb, ou, pi, gv);
                     }
-                    store_node<S>(P, og, gv);
+                    finalize_store<S>(P, og, orr, orb, oux, ouy, ouz, pi);
                 }
             }
         }
-        gather(std::integral_constant<int, 0>{}, accC);
-        gather(std::integral_constant<int, 1>{}, accN);
+        if (dest_row) {
+            gather(std::integral_constant<int, 0>{}, accC);
+            gather(std::integral_constant<int, 1>{}, accN);
+        }
         accP = accC;
         accC = accN;
         accN.zero();
