@@ -50,6 +50,11 @@ __device__ __forceinline__ long long lin(const StepParams& P, int x, int y, int 
     return static_cast<long long>(z) * P.plane + static_cast<long long>(y) * P.pitch + x;
 }
 
+// store reference moments at (x, y, z) and, on periodic x / y axes, at the ghost-layer image
+// of a first / last fluid layer (the step kernel reads wrapped sources from the ghost frame)
+template <typename S>
+__device__ __forceinline__ void store_with_images(const StepParams& P, int x, int y, int z, const float (&m)[NF]);
+
 __device__ __forceinline__ void transverse(int a, int& t0, int& t1) {
     t0 = a == 0 ? 1 : 0;
     t1 = a == 2 ? 1 : 2;
@@ -61,6 +66,39 @@ __device__ __forceinline__ float jet_mask(const StepParams& P, int u, int v) {
     const float du = __fsub_rn(static_cast<float>(u), P.jet_c0);
     const float dv = __fsub_rn(static_cast<float>(v), P.jet_c1);
     return __fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv)) <= __fmul_rn(P.jet_radius, P.jet_radius) ? 1.0f : 0.0f;
+}
+
+template <typename S>
+__device__ __forceinline__ void store_with_images(const StepParams& P, int x, int y, int z, const float (&m)[NF]) {
+    store_moments<S>(P, P.b, lin(P, x, y, z), m);
+    if (!P.ghost_images) return;
+    const int ix = P.bc[0] == MBCG_BC_PERIODIC ? (x == 1 ? P.nx - 1 : (x == P.nx - 2 ? 0 : -1)) : -1;
+    const int iy = P.bc[1] == MBCG_BC_PERIODIC ? (y == 1 ? P.ny - 1 : (y == P.ny - 2 ? 0 : -1)) : -1;
+    if (ix >= 0) store_moments<S>(P, P.b, lin(P, ix, y, z), m);
+    if (iy >= 0) store_moments<S>(P, P.b, lin(P, x, iy, z), m);
+    if (ix >= 0 && iy >= 0) store_moments<S>(P, P.b, lin(P, ix, iy, z), m);
+}
+
+// Fill the ghost frame of periodic x (axis 0) or y (axis 1) with the images of the opposite
+// fluid layer, on the state P.b: x first over every row, then y over every column, so the
+// corners hold the doubly wrapped node.
+template <typename S>
+__global__ void fill_ghosts_kernel(const StepParams P, int axis) {
+    const int n = axis == 0 ? P.nx : P.ny;
+    const int m = axis == 0 ? P.ny : P.nx; // the other in-plane axis, full extent
+    const long long total = static_cast<long long>(m) * P.nz * 2;
+    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int side = static_cast<int>(e & 1);
+        const long long r = e >> 1;
+        const int t = static_cast<int>(r % m);
+        const int z = static_cast<int>(r / m);
+        const int dst = side == 0 ? 0 : n - 1;
+        const int src = side == 0 ? n - 2 : 1;
+        const long long od = axis == 0 ? lin(P, dst, t, z) : lin(P, t, dst, z);
+        const long long os = axis == 0 ? lin(P, src, t, z) : lin(P, t, src, z);
+        for (int f = 0; f < NF; ++f) static_cast<S*>(P.b[f])[od] = static_cast<const S*>(P.b[f])[os];
+    }
 }
 
 // ---------------------------------------------------------------- inlet / outlet functors
@@ -101,7 +139,7 @@ __global__ void bc_kernel(const StepParams P, int init_inlet) {
                 for (int c = 0; c < 3; ++c) g[2 + c] += m * P.noise_amp * noise_xi(P.seed, P.step, node, c);
             }
             for (int i = 5; i < NF; ++i) g[i] = init_inlet ? 0.0f : fv[i];
-            store_moments<S>(P, P.b, ob, g);
+            store_with_images<S>(P, pb[0], pb[1], pb[2], g);
         }
         if (init_inlet) continue;
         // outlet
@@ -127,7 +165,7 @@ __global__ void bc_kernel(const StepParams P, int init_inlet) {
                 }
                 for (int i = 5; i < NF; ++i) g[i] = fv[i];
             }
-            store_moments<S>(P, P.b, ob, g);
+            store_with_images<S>(P, pb[0], pb[1], pb[2], g);
         }
     }
 }
@@ -351,6 +389,26 @@ int grid_for(long long n) {
 
 } // namespace
 
+template <typename S>
+static cudaError_t fill_ghosts_t(const StepParams& P, cudaStream_t s) {
+    for (int axis = 0; axis < 2; ++axis) {
+        if (P.bc[axis] != MBCG_BC_PERIODIC) continue;
+        const long long n = static_cast<long long>(axis == 0 ? P.ny : P.nx) * P.nz * 2;
+        fill_ghosts_kernel<S><<<grid_for(n), 256, 0, s>>>(P, axis);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_fill_ghosts(int precision, const StepParams& P, cudaStream_t s) {
+    switch (precision) {
+    case MBCG_FP16: return fill_ghosts_t<__half>(P, s);
+    case MBCG_BF16: return fill_ghosts_t<__nv_bfloat16>(P, s);
+    default: return fill_ghosts_t<float>(P, s);
+    }
+}
+
 cudaError_t launch_bc(int precision, const StepParams& P, cudaStream_t s) {
     if (P.inout_axis < 0) return cudaSuccess;
     switch (precision) {
@@ -403,8 +461,9 @@ static cudaError_t init_t(const StepParams& P, const mbcg_params& p, cudaStream_
         e = bc_t<S>(Q, 1, s);
         if (e != cudaSuccess) return e;
         e = bc_t<S>(Q, 0, s);
+        if (e != cudaSuccess) return e;
     }
-    return e;
+    return P.ghost_images ? fill_ghosts_t<S>(P, s) : e;
 }
 
 cudaError_t launch_init(int precision, const StepParams& P, const mbcg_params& p, cudaStream_t s) {

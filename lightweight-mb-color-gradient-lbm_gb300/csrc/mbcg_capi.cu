@@ -105,6 +105,7 @@ void fill_physics(const mbcg_params& p, StepParams& P) {
     P.rho_mean = static_cast<float>(0.5 * (p.rho_r0 + p.rho_b0));
     P.rho_half_diff = static_cast<float>(0.5 * (p.rho_r0 - p.rho_b0));
     P.do_bc = 1;
+    P.ghost_images = 1;
 }
 
 int choose_zchunk(const mbcg_params& p) {
@@ -119,11 +120,23 @@ int choose_zchunk(const mbcg_params& p) {
     int sms = 152;
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // aim for about four waves of one CTA per SM, with at least 16 planes per chunk
-    const long long want = 4LL * sms;
-    long long gz = (want + gx * gy - 1) / (gx * gy);
-    gz = std::max<long long>(1, std::min<long long>(gz, std::max(1, nzf / 16)));
-    return static_cast<int>((nzf + gz - 1) / gz);
+    // One CTA per SM: pick the number of z chunks that best fills whole waves, charging each
+    // chunk the three extra planes it stages before its first destination plane.
+    double best = -1.0;
+    int best_chunk = nzf;
+    for (long long gz = 1; gz <= std::max(1, nzf / 8); ++gz) {
+        const long long chunk = (nzf + gz - 1) / gz;
+        const long long gzr = (nzf + chunk - 1) / chunk;
+        const long long ctas = gx * gy * gzr;
+        const long long waves = (ctas + sms - 1) / sms;
+        const double fill = static_cast<double>(ctas) / static_cast<double>(waves * sms);
+        const double eff = fill * static_cast<double>(chunk) / static_cast<double>(chunk + 3);
+        if (eff > best + 1e-9) {
+            best = eff;
+            best_chunk = static_cast<int>(chunk);
+        }
+    }
+    return best_chunk;
 }
 
 // ---------------------------------------------------------------- tensor maps
@@ -476,6 +489,10 @@ int mbcg_copy_in(mbcg_case* c, const float* const host[MBCG_NFIELDS], mbcg_strea
         cudaFree(staging);
         if (e != cudaSuccess) return cuda_fail(e, "copy in");
     }
+    {
+        StepParams P = make_params(c, c->cur ^ 1, c->steps); // P.b = current state
+        MBCG_TRY(launch_fill_ghosts(p.precision, P, st), "ghost images");
+    }
     MBCG_TRY(cudaStreamSynchronize(st), "copy in");
     return MBCG_OK;
 }
@@ -518,6 +535,12 @@ int mbcg_rcs_moments(const mbcg_params* p, const mbcg_moments* a, const mbcg_mom
     if (a->pitch != b->pitch) return fail(MBCG_E_INVALID, "A and B must share a pitch");
     StepParams P = raw_params(p, a, b, step);
     P.do_bc = 0;
+    {
+        // the step reads wrapped sources from the ghost frame: fill it on the caller's state A
+        // (the reference never reads its periodic ghost layers, so this changes none of its data)
+        StepParams G = raw_params(p, nullptr, a, step);
+        MBCG_TRY(launch_fill_ghosts(p->precision, G, reinterpret_cast<cudaStream_t>(s)), "ghost images");
+    }
     TensorMaps T;
     std::memset(&T, 0, sizeof(T));
     const bool tma = tma_capable(*p, a->f, a->pitch, p->precision);

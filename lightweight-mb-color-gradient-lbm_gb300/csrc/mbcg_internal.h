@@ -9,7 +9,7 @@
 
 namespace mbcg {
 
-constexpr int kStepW = 10; // warps (rows) per step CTA: 8 destination rows + 2 halo rows
+constexpr int kStepW = 16; // warps (rows) per step CTA: 14 destination rows + 2 halo rows
 
 struct TensorMaps {
     CUtensorMap m[NF];
@@ -25,6 +25,7 @@ int step_m_box_x();
 
 // boundary functors, initial conditions, diagnostics, layout conversion (mbcg_aux.cu)
 cudaError_t launch_bc(int precision, const StepParams& P, cudaStream_t s);
+cudaError_t launch_fill_ghosts(int precision, const StepParams& P, cudaStream_t s); // on P.b
 cudaError_t launch_init(int precision, const StepParams& P, const mbcg_params& p, cudaStream_t s);
 cudaError_t launch_diag(int precision, const StepParams& P, const mbcg_params& p, double* partials, int nparts,
                         double* result, cudaStream_t s);

@@ -119,6 +119,8 @@ struct StepParams {
     // launch geometry
     int zchunk;         // destination planes per CTA
     int do_bc;          // fuse the inlet/outlet functors into the step
+    int ghost_images;   // the ghost frame of periodic x / y axes holds the periodic images of
+                        // the opposite fluid layer (read by the step, written through on store)
     int* status;        // device status word (bounded-wait failures); may be null
     const void* a[NF];  // current state
     void* b[NF];        // next state
@@ -141,9 +143,9 @@ MBCG_HD float noise_xi(unsigned long long seed, long long step, unsigned long lo
 // (bounds.cuh:34-77 generalised to the halo of width 2 the colour gradient needs).
 MBCG_HD int periodic_image(int p, int n) {
     const int L = n - 2;
-    int q = (p - 1) % L;
-    if (q < 0) q += L;
-    return q + 1;
+    while (p < 1) p += L;
+    while (p > n - 2) p -= L;
+    return p;
 }
 
 } // namespace mbcg

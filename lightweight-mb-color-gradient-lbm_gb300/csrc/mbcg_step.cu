@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <type_traits>
 
 #include "mbcg_lattice.cuh"
 #include "mbcg_internal.h"
@@ -141,14 +142,21 @@ struct Node {
 
 template <typename S>
 __device__ __forceinline__ float psi_of(const StepParams& P, S s0, S s1) {
-    if constexpr (sizeof(S) == 4) {
+    if constexpr (std::is_same<S, float>::value) {
         const float r = Codec<S>::to_f(s0), b = Codec<S>::to_f(s1);
-        return (r - b) / (r + b);
+        return __fdividef(r - b, r + b);
     } else {
         (void)P;
         (void)s0;
         return Codec<S>::to_f(s1);
     }
+}
+
+// psi from the two stored slots already widened to float
+template <typename S>
+__device__ __forceinline__ float psi_of_slots(float v0, float v1) {
+    if constexpr (std::is_same<S, float>::value) return __fdividef(v0 - v1, v0 + v1);
+    else return v1;
 }
 
 // decode the 11 stored slots into the reference's moments
@@ -294,17 +302,28 @@ __device__ __forceinline__ void add_pop(Acc& a, float g, float r, int ex, int ey
 // fast reciprocal (MUFU-based, <= 2 ulp); the colour fraction of a pure node stays exact
 __device__ __forceinline__ float fast_rcp(float v) { return __fdividef(1.0f, v); }
 
+// Store one node at (x, y, z); on periodic x / y axes the first and last fluid layers are also
+// written to their image in the opposite ghost layer, so the next step reads every source
+// (including wrapped ones) from the staged box (bounds.cuh:34-77 wraps on read instead).
 template <typename S>
-__device__ __forceinline__ void finalize_store(const StepParams& P, long long o, float rr, float rb, float ux,
-                                               float uy, float uz, const float (&pi)[6]) {
+__device__ __forceinline__ void finalize_store(const StepParams& P, int x, int y, int z, float rr, float rb,
+                                               float ux, float uy, float uz, const float (&pi)[6]) {
     const float u[3] = {ux, uy, uz};
     S out[NF];
     encode<S>(P, rr, rb, u, pi, out);
-    store_node<S>(P, o, out);
+    const long long zo = static_cast<long long>(z) * P.plane;
+    store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + x, out);
+    if (P.ghost_images) {
+        const int ix = P.bc[0] == MBCG_BC_PERIODIC ? (x == 1 ? P.nx - 1 : (x == P.nx - 2 ? 0 : -1)) : -1;
+        const int iy = P.bc[1] == MBCG_BC_PERIODIC ? (y == 1 ? P.ny - 1 : (y == P.ny - 2 ? 0 : -1)) : -1;
+        if (ix >= 0) store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + ix, out);
+        if (iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + x, out);
+        if (ix >= 0 && iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + ix, out);
+    }
 }
 
 template <int Q, typename S, int W, bool kTMA>
-__global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__ StepParams P,
+__global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__ StepParams P,
                                                          const __grid_constant__ TensorMaps T) {
     using G = Geo<S, W>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -337,24 +356,33 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
     const bool dest_thread = lane >= 1 && lane <= kTX && w >= 1 && w <= W - 2 && xs <= nx - 2 && ys <= ny - 2;
     const int rx = axis_role(P, 0, xs, nx);
     const int ry = axis_role(P, 1, ys, ny);
-    const bool col_in_box = (rx != R_IMAGE && ry != R_IMAGE);
+    const bool col_in_box = (rx != R_IMAGE || P.ghost_images) && (ry != R_IMAGE || P.ghost_images);
     const long long gxy = static_cast<long long>(data_coord(P, 1, ys, ny)) * P.pitch + data_coord(P, 0, xs, nx);
     const int ia = P.inout_axis;
 
-    // psi fill: each thread owns <= kPsiPer ring elements; their mapping never changes along z
+    // psi fill: each thread owns <= kPsiPer ring elements; their mapping never changes along z.
+    // Each element reads the staged box at the node whose stored value equals psi there (the
+    // periodic ghost frame holds images), or, for the periodic images two layers out that the
+    // box cannot hold, a global load issued one plane ahead into registers.
     constexpr int kPsiPer = (G::psi_plane + 32 * W - 1) / (32 * W);
-    int psi_box[kPsiPer];
-    long long psi_g[kPsiPer];
+    int psi_box[kPsiPer];      // box index, -1: prefetched global load, -2: no element
+    long long psi_g[kPsiPer];  // mapped (x, y) offset in global memory
+    float pf0[kPsiPer], pf1[kPsiPer];
 #pragma unroll
     for (int j = 0; j < kPsiPer; ++j) {
         const int e = tid + j * 32 * W;
         psi_box[j] = -2;
         psi_g[j] = 0;
+        pf0[j] = pf1[j] = 0.0f;
         if (e < G::psi_plane) {
             const int r = e / kPSX, c = e % kPSX;
             const int gx = xb - 1 + c, gy = yb - 1 + r;
             const int mx = psi_coord(P, 0, gx, nx), my = psi_coord(P, 1, gy, ny);
-            psi_box[j] = (mx == gx && my == gy) ? r * kRBX + c + offRB - 1 : -1;
+            const bool px = P.bc[0] == MBCG_BC_PERIODIC, py = P.bc[1] == MBCG_BC_PERIODIC;
+            const int dx = (px && P.ghost_images && gx >= 0 && gx <= nx - 1) ? gx : mx;
+            const int dy = (py && P.ghost_images && gy >= 0 && gy <= ny - 1) ? gy : my;
+            const int bc_ = dx - xr0, br_ = dy - (yb - 1);
+            psi_box[j] = (bc_ >= 0 && bc_ < kRBX && br_ >= 0 && br_ < G::RBY) ? br_ * kRBX + bc_ : -1;
             psi_g[j] = static_cast<long long>(my) * P.pitch + mx;
         }
     }
@@ -424,7 +452,16 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
 
     // ---- psi ring: psi = (rhor - rhob)/rho (mathUtilities.cuh:12-19) of plane k over
     // columns xb-1..xb+32 and rows yb-1..yb+W, colour-gradient neighbour rule applied
-    auto fill_psi = [&](int k) {
+    auto prefetch_psi = [&](int k) {
+        const long long zo = static_cast<long long>(psi_coord(P, 2, k, nz)) * P.plane;
+#pragma unroll
+        for (int j = 0; j < kPsiPer; ++j)
+            if (psi_box[j] == -1) {
+                pf0[j] = Codec<S>::to_f(static_cast<const S*>(P.a[0])[zo + psi_g[j]]);
+                pf1[j] = Codec<S>::to_f(static_cast<const S*>(P.a[1])[zo + psi_g[j]]);
+            }
+    };
+    auto fill_psi = [&](int k, bool prefetched) {
         float* ring = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
         const int mz = psi_coord(P, 2, k, nz);
         const bool plane_in_box = (mz == zload(k));
@@ -438,6 +475,8 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
             float v;
             if (plane_in_box && psi_box[j] >= 0) {
                 v = psi_of<S>(P, r0b[psi_box[j]], r1b[psi_box[j]]);
+            } else if (prefetched && psi_box[j] == -1) {
+                v = psi_of_slots<S>(pf0[j], pf1[j]);
             } else {
                 const long long o = zo + psi_g[j];
                 v = psi_of<S>(P, static_cast<const S*>(P.a[0])[o], static_cast<const S*>(P.a[1])[o]);
@@ -464,8 +503,9 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
             return;
         }
     }
-    fill_psi(kfirst);
-    fill_psi(kfirst + 1);
+    fill_psi(kfirst, false);
+    fill_psi(kfirst + 1, false);
+    prefetch_psi(kfirst + 2);
 
     Acc accP, accC, accN; // destination planes k-1, k, k+1
     accP.zero();
@@ -485,7 +525,8 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
                 return;
             }
         }
-        fill_psi(k + 1);
+        fill_psi(k + 1, true);
+        if (k + 2 <= zd1 + 1) prefetch_psi(k + 2);
         __syncthreads();
         // (2) prefetch plane k+2 into the slot plane k-1 used
         if (k + 2 <= zd1 + 1 && k + 2 > k_issued) {
@@ -615,10 +656,9 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
             }
         }
 
-        // separable inverse transform: x-pass t_bc(cx), y-pass s_c(cx, cy); e = s0 + s2
-        float s0[3][3], s1[3][3], e2[3][3];
+        // separable inverse transform, x-pass: t_bc(cx) for the monomials cy^b cz^c
+        float t00[3], t10[3], t01[3], t20[3], t02[3], t11[3];
         {
-            float t00[3], t10[3], t01[3], t20[3], t02[3], t11[3];
             const float a = cf.p000 + cf.p200;
             t00[1] = cf.p000; t00[2] = a + cf.p100; t00[0] = a - cf.p100;
             const float b = cf.p010 + cf.p210;
@@ -628,21 +668,15 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
             t20[1] = cf.p020; t20[2] = cf.p020 + cf.p120; t20[0] = cf.p020 - cf.p120;
             t02[1] = cf.p002; t02[2] = cf.p002 + cf.p102; t02[0] = cf.p002 - cf.p102;
             t11[1] = cf.p011; t11[2] = cf.p011 + cf.p111; t11[0] = cf.p011 - cf.p111;
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                const float e0 = t00[i] + t20[i];
-                s0[i][1] = t00[i]; s0[i][2] = e0 + t10[i]; s0[i][0] = e0 - t10[i];
-                const float e1 = t01[i] + cf.p021;
-                s1[i][1] = t01[i]; s1[i][2] = e1 + t11[i]; s1[i][0] = e1 - t11[i];
-                e2[i][1] = s0[i][1] + t02[i];
-                e2[i][2] = s0[i][2] + (t02[i] + cf.p012);
-                e2[i][0] = s0[i][0] + (t02[i] - cf.p012);
-            }
         }
-        // recolouring strength per shell, d_s = dcoef * w_s / |c|
-        const float dk1 = dcoef * weight<Q>(1, 0, 0);
-        const float dk2 = dcoef * weight<Q>(1, 1, 0) * 0.7071067811865475f;
-        const float dk3 = dcoef * weight<Q>(1, 1, 1) * 0.5773502691896258f;
+        // D3Q27 weights are separable, w(c) = prod over axes of (1/6)(4 if c_a = 0): populations
+        // are carried unweighted and the axis factors are applied inside the forward passes,
+        // the common 1/216 once per destination.  D3Q19 weights are applied per population.
+        constexpr bool kSepW = (Q == 27);
+        const float dk1 = kSepW ? dcoef : dcoef * weight<Q>(1, 0, 0);
+        const float dk2 = (kSepW ? dcoef : dcoef * weight<Q>(1, 1, 0)) * 0.7071067811865475f;
+        const float dk3 = kSepW ? dcoef * 0.5773502691896258f : 0.0f;
+        const float rc0 = kSepW ? cf.r0 * (1.0f / w0) : cf.r0;
 
         // wall bounce-back of this node's own populations (destination = this node, plane k)
         const bool wx0 = P.bc[0] == MBCG_BC_WALL && xs == 1, wx1 = P.bc[0] == MBCG_BC_WALL && xs == nx - 2;
@@ -651,106 +685,152 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
         const bool reflect = role == R_FLUID && dest_thread && (wx0 | wx1 | wy0 | wy1 | wz0 | wz1);
         const bool any_reflect = __any_sync(kFull, reflect);
 
-        // ---- per class cz: populations, x streaming, own-row moments, y exchange ----
-        auto do_class = [&](auto czc, Acc& acc) {
-            constexpr int cz = decltype(czc)::value;
-            float g[3][3], r[3][3];
+        // ---- emit: populations of the rows this warp exports, x streaming, own-row moments,
+        // y exchange.  Halo rows export one population row (cy = +1 for warp 0, -1 for warp W-1).
+        auto emit = [&](auto rowsc) {
+            constexpr int ROWS = decltype(rowsc)::value;
+            float s0[3][3], s1[3][3], e2[3][3];
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const int cx = i - 1, cy = j - 1;
-                    if (!Stencil<Q>::has(cx, cy, cz)) {
-                        g[i][j] = 0.0f;
-                        continue;
-                    }
-                    const float vv = cz == 0 ? s0[i][j] : (cz > 0 ? e2[i][j] + s1[i][j] : e2[i][j] - s1[i][j]);
-                    float gi = weight<Q>(cx, cy, cz) * vv;
-                    if (cx == 0 && cy == 0 && cz == 0) gi += cf.r0;
-                    g[i][j] = gi;
+                const float e0 = t00[i] + t20[i];
+                const float e1 = t01[i] + cf.p021;
+                if (ROWS & 2) {
+                    s0[i][1] = t00[i];
+                    s1[i][1] = t01[i];
+                    e2[i][1] = t00[i] + t02[i];
+                }
+                if (ROWS & 4) {
+                    s0[i][2] = e0 + t10[i];
+                    s1[i][2] = e1 + t11[i];
+                    e2[i][2] = s0[i][2] + (t02[i] + cf.p012);
+                }
+                if (ROWS & 1) {
+                    s0[i][0] = e0 - t10[i];
+                    s1[i][0] = e1 - t11[i];
+                    e2[i][0] = s0[i][0] + (t02[i] - cf.p012);
                 }
             }
-            if (any_iface) {
+            auto do_class = [&](auto czc, Acc& acc) {
+                constexpr int cz = decltype(czc)::value;
+                float g[3][3], r[3][3];
 #pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) {
-                        const int cx = i - 1, cy = j - 1, sh = cx * cx + cy * cy + cz * cz;
-                        const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
-                        const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
-                        r[i][j] = sh == 0 ? aR * g[i][j] : fmaf(aR, g[i][j], dks * fc);
-                    }
-            } else {
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) r[i][j] = aR * g[i][j];
-            }
-            if (any_reflect && reflect) {
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
+                for (int i = 0; i < 3; ++i) {
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
                         const int cx = i - 1, cy = j - 1;
-                        if (!Stencil<Q>::has(cx, cy, cz)) continue;
-                        const bool into = (wx0 && cx < 0) || (wx1 && cx > 0) || (wy0 && cy < 0) || (wy1 && cy > 0) ||
-                                          (wz0 && cz < 0) || (wz1 && cz > 0);
-                        if (into) add_pop(accC, g[i][j], r[i][j], -cx, -cy, -cz);
+                        g[i][j] = 0.0f;
+                        r[i][j] = 0.0f;
+                        if (!(ROWS & (1 << j)) || !Stencil<Q>::has(cx, cy, cz)) continue;
+                        const float vv =
+                            cz == 0 ? s0[i][j] : (cz > 0 ? e2[i][j] + s1[i][j] : e2[i][j] - s1[i][j]);
+                        float gi = kSepW ? vv : weight<Q>(cx, cy, cz) * vv;
+                        if (cx == 0 && cy == 0 && cz == 0) gi += rc0;
+                        g[i][j] = gi;
                     }
-            }
-            // x streaming: destination x receives cx=+1 from lane-1 and cx=-1 from lane+1
-            float X0[3], X1[3], X2[3], XR[3];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int cy = j - 1;
-                if (Stencil<Q>::has(1, cy, cz)) {
-                    const float gl = __shfl_up_sync(kFull, g[2][j], 1);
-                    const float gr = __shfl_down_sync(kFull, g[0][j], 1);
-                    const float rl = __shfl_up_sync(kFull, r[2][j], 1);
-                    const float rr_ = __shfl_down_sync(kFull, r[0][j], 1);
-                    X2[j] = gl + gr;
-                    X0[j] = X2[j] + g[1][j];
-                    X1[j] = gl - gr;
-                    XR[j] = (rl + rr_) + r[1][j];
-                } else {
-                    X0[j] = g[1][j];
-                    X1[j] = 0.0f;
-                    X2[j] = 0.0f;
-                    XR[j] = r[1][j];
                 }
-            }
-            // cy = 0 row stays in this column: add to the destination's sums now
-            acc.rho += X0[1];
-            acc.jx += X1[1];
-            acc.xx += X2[1];
-            acc.red += XR[1];
-            if (cz != 0) {
-                acc.jz += cz * X0[1];
-                acc.xz += cz * X1[1];
-                acc.zz += X0[1];
-            }
-            // cy = +1 goes to row w+1 (slot 0), cy = -1 to row w-1 (slot 1)
-            constexpr int cls = cz + 1;
-            float* b0 = xb_self + ((cls * 2 + 0) * 4) * (W * 32);
-            float* b1 = xb_self + ((cls * 2 + 1) * 4) * (W * 32);
-            b0[0 * W * 32] = X0[2];
-            b0[1 * W * 32] = X1[2];
-            b0[2 * W * 32] = X2[2];
-            b0[3 * W * 32] = XR[2];
-            b1[0 * W * 32] = X0[0];
-            b1[1 * W * 32] = X1[0];
-            b1[2 * W * 32] = X2[0];
-            b1[3 * W * 32] = XR[0];
+                {
+                    if (any_iface) {
+#pragma unroll
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) {
+                                const int cx = i - 1, cy = j - 1, sh = cx * cx + cy * cy + cz * cz;
+                                if (!(ROWS & (1 << j))) continue;
+                                const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
+                                const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
+                                r[i][j] = sh == 0 ? aR * g[i][j] : fmaf(aR, g[i][j], dks * fc);
+                            }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int j = 0; j < 3; ++j)
+                                if (ROWS & (1 << j)) r[i][j] = aR * g[i][j];
+                    }
+                }
+                if constexpr (ROWS == 7) {
+                    if (any_reflect && reflect) {
+#pragma unroll
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) {
+                                const int cx = i - 1, cy = j - 1;
+                                if (!Stencil<Q>::has(cx, cy, cz)) continue;
+                                const bool into = (wx0 && cx < 0) || (wx1 && cx > 0) || (wy0 && cy < 0) ||
+                                                  (wy1 && cy > 0) || (wz0 && cz < 0) || (wz1 && cz > 0);
+                                if (!into) continue;
+                                const float f = kSepW ? static_cast<float>((cx == 0 ? 4 : 1) * (cy == 0 ? 4 : 1) *
+                                                                           (cz == 0 ? 4 : 1))
+                                                      : 1.0f;
+                                add_pop(accC, f * g[i][j], f * r[i][j], -cx, -cy, -cz);
+                            }
+                    }
+                }
+                // x streaming: destination x receives cx=+1 from lane-1 and cx=-1 from lane+1
+                float X0[3], X1[3], X2[3], XR[3];
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    const int cy = j - 1;
+                    X0[j] = X1[j] = X2[j] = XR[j] = 0.0f;
+                    if (!(ROWS & (1 << j))) continue;
+                    if (Stencil<Q>::has(1, cy, cz)) {
+                        const float gl = __shfl_up_sync(kFull, g[2][j], 1);
+                        const float gr = __shfl_down_sync(kFull, g[0][j], 1);
+                        X2[j] = gl + gr;
+                        X0[j] = kSepW ? fmaf(4.0f, g[1][j], X2[j]) : X2[j] + g[1][j];
+                        X1[j] = gl - gr;
+                        const float rl = __shfl_up_sync(kFull, r[2][j], 1);
+                        const float rr_ = __shfl_down_sync(kFull, r[0][j], 1);
+                        XR[j] = kSepW ? fmaf(4.0f, r[1][j], rl + rr_) : (rl + rr_) + r[1][j];
+                    } else {
+                        X0[j] = g[1][j];
+                        XR[j] = r[1][j];
+                    }
+                }
+                if constexpr ((ROWS & 2) != 0) {
+                    // cy = 0 row stays in this column: add to the destination's sums now
+                    constexpr float f = kSepW ? (cz == 0 ? 16.0f : 4.0f) : 1.0f;
+                    acc.rho = fmaf(f, X0[1], acc.rho);
+                    acc.jx = fmaf(f, X1[1], acc.jx);
+                    acc.xx = fmaf(f, X2[1], acc.xx);
+                    acc.red = fmaf(f, XR[1], acc.red);
+                    if (cz != 0) {
+                        acc.jz = fmaf(cz * f, X0[1], acc.jz);
+                        acc.xz = fmaf(cz * f, X1[1], acc.xz);
+                        acc.zz = fmaf(f, X0[1], acc.zz);
+                    }
+                }
+                // cy = +1 goes to row w+1 (slot 0), cy = -1 to row w-1 (slot 1)
+                constexpr int cls = cz + 1;
+                if constexpr ((ROWS & 4) != 0) {
+                    float* b0 = xb_self + ((cls * 2 + 0) * 4) * (W * 32);
+                    b0[0 * W * 32] = X0[2];
+                    b0[1 * W * 32] = X1[2];
+                    b0[2 * W * 32] = X2[2];
+                    b0[3 * W * 32] = XR[2];
+                }
+                if constexpr ((ROWS & 1) != 0) {
+                    float* b1 = xb_self + ((cls * 2 + 1) * 4) * (W * 32);
+                    b1[0 * W * 32] = X0[0];
+                    b1[1 * W * 32] = X1[0];
+                    b1[2 * W * 32] = X2[0];
+                    b1[3 * W * 32] = XR[0];
+                }
+            };
+            do_class(std::integral_constant<int, -1>{}, accP);
+            do_class(std::integral_constant<int, 0>{}, accC);
+            do_class(std::integral_constant<int, 1>{}, accN);
         };
-        do_class(std::integral_constant<int, -1>{}, accP);
-        do_class(std::integral_constant<int, 0>{}, accC);
-        do_class(std::integral_constant<int, 1>{}, accN);
+        if (w == 0) emit(std::integral_constant<int, 4>{});
+        else if (w == W - 1) emit(std::integral_constant<int, 1>{});
+        else emit(std::integral_constant<int, 7>{});
         __syncthreads();
 
         // (4) y streaming into destination rows
         auto gather = [&](auto czc, Acc& acc) {
             constexpr int cz = decltype(czc)::value;
             constexpr int cls = cz + 1;
+            constexpr float f = (kSepW && cz == 0) ? 4.0f : 1.0f;
             const float* p0 = xb_self - 32 + ((cls * 2 + 0) * 4) * (W * 32);
             const float* m1 = xb_self + 32 + ((cls * 2 + 1) * 4) * (W * 32);
             const float P0 = p0[0], P1 = p0[W * 32], P2 = p0[2 * W * 32], PR = p0[3 * W * 32];
@@ -758,13 +838,13 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
             const float s00 = P0 + M0;
             const float s10 = P1 + M1;
             const float d00 = P0 - M0;
-            acc.rho += s00;
-            acc.jx += s10;
-            acc.xx += P2 + M2;
-            acc.jy += d00;
-            acc.xy += P1 - M1;
-            acc.yy += s00;
-            acc.red += PR + MR;
+            acc.rho = fmaf(f, s00, acc.rho);
+            acc.jx = fmaf(f, s10, acc.jx);
+            acc.xx = fmaf(f, P2 + M2, acc.xx);
+            acc.jy = fmaf(f, d00, acc.jy);
+            acc.xy = fmaf(f, P1 - M1, acc.xy);
+            acc.yy = fmaf(f, s00, acc.yy);
+            acc.red = fmaf(f, PR + MR, acc.red);
             if (cz != 0) {
                 acc.jz += cz * s00;
                 acc.xz += cz * s10;
@@ -778,6 +858,11 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
         // (5) destination plane k-1 is complete: moments (lbm.cuh:239-261), store, boundary
         const int d = k - 1;
         if (dest_thread && d >= zd0 && d < zd1) {
+            if constexpr (kSepW) {
+                constexpr float sc = 1.0f / 216.0f;
+                accP.rho *= sc; accP.red *= sc; accP.jx *= sc; accP.jy *= sc; accP.jz *= sc;
+                accP.xx *= sc; accP.xy *= sc; accP.yy *= sc; accP.yz *= sc; accP.zz *= sc; accP.xz *= sc;
+            }
             const float rho = accP.rho;
             const float rr = accP.red;
             const float rb = rho - rr;
@@ -813,8 +898,7 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
                 pi[2] -= Kc;
                 pi[4] -= Kc;
             }
-            const long long o = static_cast<long long>(d) * P.plane + static_cast<long long>(ys) * P.pitch + xs;
-            finalize_store<S>(P, o, rr, rb, ux, uy, uz, pi);
+            finalize_store<S>(P, xs, ys, d, rr, rb, ux, uy, uz, pi);
 
             if (P.do_bc && ia >= 0) {
                 // inlet / outlet functors fused into the first and last fluid layer
@@ -877,7 +961,7 @@ __global__ void __launch_bounds__(32 * W, 2) step_kernel(const __grid_constant__
                             ouz = on.uz - uc * (on.uz - uz);
                         }
                     }
-                    finalize_store<S>(P, og, orr, orb, oux, ouy, ouz, pi);
+                    finalize_store<S>(P, gx, gy, gz, orr, orb, oux, ouy, ouz, pi);
                 }
             }
         }

@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#ifndef __CUDACC__
 #undef __host__
 #undef __device__
 #undef __global__
@@ -22,6 +23,7 @@
 #define __device__
 #define __global__
 #define __forceinline__ inline
+#endif
 
 #ifndef REF_REAL
 #define REF_REAL float
