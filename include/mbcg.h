@@ -96,7 +96,10 @@ typedef struct mbcg_params {
     double rti_width;
     double rti_phase_above; /* phi above the interface: -1 = blue (reference), +1 = red    */
     int32_t rti_mode[2];    /* modes along the two transverse axes, in axis order          */
-    int32_t reserved0;
+    int32_t omega2_conservative; /* 0 (reference): below |F| = 1e-4 cos2rule is 0 but Omega2
+                               still subtracts A|F|B_i/2, which does not sum to zero
+                               (forces.cuh:80-83, collisionOperators.cuh:16-25); 1: Omega2 is
+                               zero there, so colour masses are conserved exactly          */
     int32_t reserved1;
     /* FP16/BF16 storage scales */
     double rho_scale;       /* (rho - rho_nominal) / rho_scale is stored; default 0.01     */

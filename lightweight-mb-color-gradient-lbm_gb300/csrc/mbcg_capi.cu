@@ -81,6 +81,7 @@ void fill_physics(const mbcg_params& p, StepParams& P) {
     const float s4 = static_cast<float>(p.sigma) / (4.0f * cs4);
     P.A = s4 / taub;
     P.beta = static_cast<float>(p.beta);
+    P.omega2_conservative = p.omega2_conservative != 0;
     P.ratio = p.rho_r0 != p.rho_b0;
     const double rmin = std::min(p.rho_r0, p.rho_b0);
     P.kappa_r = static_cast<float>(rmin / p.rho_r0 - 1.0);

@@ -103,6 +103,7 @@ struct StepParams {
     float oms;          // 1 - 1/tau (constants.cuh:85)
     float A;            // sigma / (4 cs^4 tau) (forces.cuh:114-117, 132-134)
     float beta;
+    int omega2_conservative; // Omega2 = 0 below |F| = 1e-4 (mass conserving option)
     int ratio;          // density-ratio rest population on
     float kappa_r, kappa_b;
     int forced;         // body force on

@@ -228,7 +228,9 @@ __device__ __forceinline__ void build_coef(const StepParams& P, Coef& c, float r
     const float a3yzz = pzz * vy + 2.0f * pyz * vz;
     const float a3xyz = pxy * vz + pxz * vy + pyz * vx;
     const float o45 = 4.5f * oms, o9 = 9.0f * oms, o135 = 13.5f * oms;
-    c.p000 = rho * (1.0f - 1.5f * usq) - 1.5f * oms * (pxx + pyy + pzz);
+    // p000 holds only the small isotropic part; rho itself is added to every direction last
+    // (see emit), so the rounding of rho + small treats rest and moving populations alike
+    c.p000 = -1.5f * (rho * usq + oms * (pxx + pyy + pzz));
     c.p100 = rux * t1 + 4.5f * rux * ux * ux - o45 * (a3xyy + a3xzz);
     c.p010 = ruy * t1 + 4.5f * ruy * uy * uy - o45 * (a3xxy + a3yzz);
     c.p001 = ruz * t1 + 4.5f * ruz * uz * uz - o45 * (a3xxz + a3yyz);
@@ -591,12 +593,17 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
 
         // coefficient tensor and colour split; inactive sources keep all-zero coefficients
         Coef cf{};
-        float aR = 0.0f, dcoef = 0.0f, Fx = 0.0f, Fy = 0.0f, Fz = 0.0f;
+        float aR = 0.0f, dcoef = 0.0f, Fx = 0.0f, Fy = 0.0f, Fz = 0.0f, omega2_rest = 0.0f;
         bool iface = false;
         if (active) {
             const float rho = nd.rr + nd.rb;
             const float inv = fast_rcp(rho);
-            aR = nd.rb == 0.0f ? 1.0f : (nd.rr == 0.0f ? 0.0f : nd.rr * inv);
+            // colour fraction as a correctly rounded quotient (one residual correction): a
+            // product with a rounded reciprocal is biased (aR rho - rr averages +2.5e-10 per
+            // mixed node), which would move colour mass the same way every step
+            const float q0 = nd.rr * inv;
+            const float q1 = fmaf(fmaf(-q0, rho, nd.rr), inv, q0);
+            aR = nd.rb == 0.0f ? 1.0f : (nd.rr == 0.0f ? 0.0f : q1);
             if (role == R_FLUID) {
                 iface = (4.0f * nd.rr * nd.rb * inv * inv) > 1.0e-4f; // lbm.cuh:181,187
                 build_coef(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, nd.ux, nd.uy, nd.uz, nd.pxx, nd.pxy,
@@ -635,12 +642,13 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
             Fz = 3.0f * sz;
             const float absF = sqrtf(Fx * Fx + Fy * Fy + Fz * Fz);
             // Omega2 (collisionOperators.cuh:16-25) folded into the coefficients
-            const float hA = 0.5f * P.A * absF;
-            cf.p000 -= hA;
-            cf.r0 -= hA * (Stencil<Q>::B0 - w0);
+            float hA = (P.omega2_conservative && !(absF > 1.0e-4f)) ? 0.0f : 0.5f * P.A * absF;
             if (absF > 1.0e-4f) {
                 const float ia_ = fast_rcp(absF);
                 const float qf = 0.5f * P.A * ia_;
+                // isotropic part from the same q |F|^2 as the anisotropic part, so Omega2 sums
+                // to zero over the directions in floating point too
+                hA = qf * (Fx * Fx + Fy * Fy + Fz * Fz);
                 cf.p200 += qf * Fx * Fx;
                 cf.p020 += qf * Fy * Fy;
                 cf.p002 += qf * Fz * Fz;
@@ -654,7 +662,10 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
                 const float irho = fast_rcp(rho);
                 dcoef = P.beta * (nd.rr * nd.rb) * irho * irho * ia_ * feq0;
             }
+            cf.p000 -= hA;
+            omega2_rest = hA; // rest-population part, -hA (B0 - w0) = +2/3 hA, added below in exact units
         }
+        const float rho_src = active ? nd.rr + nd.rb : 0.0f;
 
         // separable inverse transform, x-pass: t_bc(cx) for the monomials cy^b cz^c
         float t00[3], t10[3], t01[3], t20[3], t02[3], t11[3];
@@ -669,14 +680,23 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
             t02[1] = cf.p002; t02[2] = cf.p002 + cf.p102; t02[0] = cf.p002 - cf.p102;
             t11[1] = cf.p011; t11[2] = cf.p011 + cf.p111; t11[0] = cf.p011 - cf.p111;
         }
-        // D3Q27 weights are separable, w(c) = prod over axes of (1/6)(4 if c_a = 0): populations
-        // are carried unweighted and the axis factors are applied inside the forward passes,
-        // the common 1/216 once per destination.  D3Q19 weights are applied per population.
+        // Populations are carried scaled by S = 216 (D3Q27) or 36 (D3Q19), where the weights
+        // are small integers that sum to S exactly: float-rounded weights do not sum to 1, and
+        // that error would scale every node's mass each step (about 1.5e-8 per step for D3Q19).
+        // D3Q27 weights are also separable, S w(c) = prod over axes of (4 if c_a = 0 else 1):
+        // populations are carried unweighted and the factors 4 are applied inside the forward
+        // passes.  D3Q19 weights 12, 2, 1 are applied per population.  Each destination
+        // divides its sums by S once, the mass sums with a correctly rounded quotient.
         constexpr bool kSepW = (Q == 27);
-        const float dk1 = kSepW ? dcoef : dcoef * weight<Q>(1, 0, 0);
-        const float dk2 = (kSepW ? dcoef : dcoef * weight<Q>(1, 1, 0)) * 0.7071067811865475f;
+        const float dk1 = kSepW ? dcoef : 2.0f * dcoef;
+        const float dk2 = dcoef * 0.7071067811865475f;
         const float dk3 = kSepW ? dcoef * 0.5773502691896258f : 0.0f;
-        const float rc0 = kSepW ? cf.r0 * (1.0f / w0) : cf.r0;
+        // rest-population correction (density-ratio K and the Omega2 rest term), with the Omega2
+        // part in exact units so that Omega2 sums to zero over the directions (B0 - w0 = -2/3
+        // for both lattices)
+        // in value units before the rest weight (64 of 216, or 12 of 36): S r0 / W_0 and
+        // S (w0 - B0) hA / W_0 = (2/3) S hA / W_0, i.e. 3.375 r0 + 2.25 hA or 3 r0 + 2 hA
+        const float rc0 = kSepW ? fmaf(cf.r0, 3.375f, 2.25f * omega2_rest) : fmaf(cf.r0, 3.0f, 2.0f * omega2_rest);
 
         // wall bounce-back of this node's own populations (destination = this node, plane k)
         const bool wx0 = P.bc[0] == MBCG_BC_WALL && xs == 1, wx1 = P.bc[0] == MBCG_BC_WALL && xs == nx - 2;
@@ -721,11 +741,12 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
                         g[i][j] = 0.0f;
                         r[i][j] = 0.0f;
                         if (!(ROWS & (1 << j)) || !Stencil<Q>::has(cx, cy, cz)) continue;
-                        const float vv =
+                        float small =
                             cz == 0 ? s0[i][j] : (cz > 0 ? e2[i][j] + s1[i][j] : e2[i][j] - s1[i][j]);
-                        float gi = kSepW ? vv : weight<Q>(cx, cy, cz) * vv;
-                        if (cx == 0 && cy == 0 && cz == 0) gi += rc0;
-                        g[i][j] = gi;
+                        if (cx == 0 && cy == 0 && cz == 0) small += rc0;
+                        const float vv = rho_src + small;
+                        const int sh = cx * cx + cy * cy + cz * cz;
+                        g[i][j] = kSepW ? vv : (sh == 0 ? 12.0f * vv : (sh == 1 ? vv + vv : vv));
                     }
                 }
                 {
@@ -858,9 +879,14 @@ __global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__
         // (5) destination plane k-1 is complete: moments (lbm.cuh:239-261), store, boundary
         const int d = k - 1;
         if (dest_thread && d >= zd0 && d < zd1) {
-            if constexpr (kSepW) {
-                constexpr float sc = 1.0f / 216.0f;
-                accP.rho *= sc; accP.red *= sc; accP.jx *= sc; accP.jy *= sc; accP.jz *= sc;
+            {
+                constexpr float S = kSepW ? 216.0f : 36.0f;
+                constexpr float sc = 1.0f / S;
+                // correctly rounded mass quotients (no systematic bias), plain scaling for the rest
+                const float q0 = accP.rho * sc, q1 = accP.red * sc;
+                accP.rho = fmaf(fmaf(-q0, S, accP.rho), sc, q0);
+                accP.red = fmaf(fmaf(-q1, S, accP.red), sc, q1);
+                accP.jx *= sc; accP.jy *= sc; accP.jz *= sc;
                 accP.xx *= sc; accP.xy *= sc; accP.yy *= sc; accP.yz *= sc; accP.zz *= sc; accP.xz *= sc;
             }
             const float rho = accP.rho;

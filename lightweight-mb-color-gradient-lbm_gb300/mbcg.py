@@ -59,7 +59,7 @@ class Params(ctypes.Structure):
         ("rti_width", ctypes.c_double),
         ("rti_phase_above", ctypes.c_double),
         ("rti_mode", ctypes.c_int32 * 2),
-        ("reserved0", ctypes.c_int32),
+        ("omega2_conservative", ctypes.c_int32),
         ("reserved1", ctypes.c_int32),
         ("rho_scale", ctypes.c_double),
         ("u_ref", ctypes.c_double),
@@ -143,7 +143,8 @@ def reference_jet_params(nx: int, ny: int, nz: int, q: int = 27, tau: float = 1.
 
 
 def bubble_params(L: int = 64, q: int = 19, radius: Optional[float] = None, width: float = 3.0,
-                  tau: float = 0.8, sigma: float = 0.01, beta: float = 0.7, precision: int = FP32) -> Params:
+                  tau: float = 0.8, sigma: float = 0.01, beta: float = 0.7, precision: int = FP32,
+                  conservative: bool = False) -> Params:
     """Static-bubble Laplace case: L^3 fluid nodes, fully periodic, phi = +1 (red) inside a
     sphere of radius L/4 centred in the box, tanh profile of the given width, rho = 1."""
     p = default_params()
@@ -159,6 +160,7 @@ def bubble_params(L: int = 64, q: int = 19, radius: Optional[float] = None, widt
     p.bubble_width = width
     p.bubble_phase = 1.0
     p.precision = precision
+    p.omega2_conservative = 1 if conservative else 0
     return p
 
 

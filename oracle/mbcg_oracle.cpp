@@ -302,7 +302,7 @@ struct Oracle {
             force(n, Fx, Fy, Fz);
             const R Acoef = k.sigma_over_4cs4 / k.taub;
             const R absF = my_sqrt(Fx * Fx + Fy * Fy + Fz * Fz);
-            gi += omega2(i, Fx, Fy, Fz, absF, Acoef);
+            if (!p.omega2_conservative || absF > static_cast<R>(1.0e-4)) gi += omega2(i, Fx, Fy, Fz, absF, Acoef);
             Deltai = recolor(i, rhor_s, rhob_s, Fx, Fy, Fz, absF);
         }
         fr = aR * gi + Deltai;
