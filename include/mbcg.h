@@ -180,6 +180,19 @@ int mbcg_bc_moments(const mbcg_params *p, const mbcg_moments *b, const mbcg_mome
  * initial boundary pass for the jet (main.cu:25-26). */
 int mbcg_init_moments(const mbcg_params *p, const mbcg_moments *a, mbcg_stream_t s);
 
+/* FP64 diagnostics of caller-owned moment arrays (reference layout, any pitch >= nx) that
+ * allocate no memory, host or device.  No counterpart in the reference: it is for callers that
+ * cannot allocate where they need the numbers -- solver loops whose device memory is entirely
+ * taken by resident states, programs whose framework allocator owns the GPU (a cudaMalloc can
+ * synchronise the device or fail under memory pressure), or code holding only MomentsDevice-style
+ * arrays and no case handle.  The partial sums live in one fixed array compiled into the library
+ * (about 385 KB, held on every GPU that loads it until the process exits); lattices above
+ * 134,217,728 fluid nodes are rejected with MBCG_E_UNSUPPORTED.  The first call on each device
+ * looks up that array's device address (with the device current), so make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race, so serialise them
+ * (same stream, or synchronise between them).  Synchronous: returns once *out is filled. */
+int mbcg_diagnostics_static(const mbcg_params *p, const mbcg_moments *a, mbcg_diag *out, mbcg_stream_t s);
+
 /* Active (fluid) node count used by the MLUPS definition, (nx-2)(ny-2)(nz-2)
  * (utilities/mlups_count.cuh:24-29). */
 int64_t mbcg_active_nodes(const mbcg_params *p);

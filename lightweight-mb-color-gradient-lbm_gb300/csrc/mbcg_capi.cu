@@ -192,6 +192,8 @@ int encode_maps(const mbcg_params& p, const void* const* f, long long pitch, int
 
 } // namespace
 
+void mbcg::set_last_error(const std::string& msg) { g_err = msg; }
+
 struct mbcg_case {
     mbcg_params p;
     int es = 4;

@@ -4,6 +4,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "mbcg.h"
 #include "mbcg_lattice.cuh"
 
@@ -34,6 +36,9 @@ cudaError_t launch_to_dense(int precision, const StepParams& P, int field, const
                             cudaStream_t s);
 cudaError_t launch_from_dense(int precision, const StepParams& P, int field, const float* src, void* dst,
                               cudaStream_t s);
+
+// sets the message mbcg_last_error() returns on the calling thread (mbcg_capi.cu)
+void set_last_error(const std::string& msg);
 
 constexpr int kDiagSlots = 12; // mass_r, mass_b, mom x/y/z, p_in sum, n_in, p_out sum, n_out, nonfinite, nodes, spare
 

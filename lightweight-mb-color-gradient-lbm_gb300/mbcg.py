@@ -264,6 +264,7 @@ _PROTOS = {
     "mbcg_bc_moments": (ctypes.c_int, [_P(Params), _P(Moments), _P(Moments), ctypes.c_int64, _VP]),
     "mbcg_init_moments": (ctypes.c_int, [_P(Params), _P(Moments), _VP]),
     "mbcg_active_nodes": (ctypes.c_int64, [_P(Params)]),
+    "mbcg_diagnostics_static": (ctypes.c_int, [_P(Params), _P(Moments), _P(Diag), _VP]),
     "mbcg_launches_per_step": (ctypes.c_int32, [_VP]),
     "mbcg_last_error": (ctypes.c_char_p, []),
     "mbcg_version": (ctypes.c_char_p, []),
