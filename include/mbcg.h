@@ -168,6 +168,19 @@ int mbcg_diagnostics(mbcg_case *c, mbcg_diag *out, mbcg_stream_t s);
 /* Reads and clears the device status word (non-zero = a bounded wait gave up). */
 int mbcg_status(mbcg_case *c, int32_t *status);
 
+/* ---- launch shape (no counterpart in the reference, whose block is the compile-time
+ * 32x4x2 of compile.sh:34-36) --------------------------------------------------------- */
+/* Step CTA shape: block_rows warps (8 or 16) of 32 lanes; zchunk destination planes per CTA
+ * along z.  mbcg_create picks a shape from a wave-filling model, or the shape an earlier
+ * mbcg_autotune measured for the same lattice, precision, sizes and boundary features. */
+int mbcg_get_shape(const mbcg_case *c, int32_t *block_rows, int32_t *zchunk);
+int mbcg_set_shape(mbcg_case *c, int32_t block_rows, int32_t zchunk);
+/* Times `repeats` steps for each candidate shape (both block shapes, several z depths) on this
+ * case, keeps the fastest and records it for later cases with the same key.  The timed steps
+ * read the current state and write the other one: the current state is unchanged.
+ * *best_ms (may be null) receives the time of one step with the chosen shape.  Synchronous. */
+int mbcg_autotune(mbcg_case *c, int32_t repeats, double *best_ms, mbcg_stream_t s);
+
 /* ---- raw entry points on caller-owned moment arrays -------------------------------- */
 /* launch_RCS(A, B, cfg) (launch.cuh:89-94) on arrays laid out as in the reference
  * (any pitch >= nx).  step is the index of the state B will hold (inlet noise key). */

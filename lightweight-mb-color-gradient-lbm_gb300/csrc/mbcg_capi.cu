@@ -13,8 +13,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "mbcg_internal.h"
 
@@ -109,20 +112,21 @@ void fill_physics(const mbcg_params& p, StepParams& P) {
     P.ghost_images = 1;
 }
 
-int choose_zchunk(const mbcg_params& p) {
+int choose_zchunk(const mbcg_params& p, int W) {
     if (const char* env = std::getenv("MBCG_ZCHUNK")) {
         const int v = std::atoi(env);
         if (v > 0) return v;
     }
-    const int W = step_box_rows();
-    const long long gx = (p.nx - 2 + step_tile_x() - 1) / step_tile_x();
+    const long long gx = (p.nx - 2 + kStepTileX - 1) / kStepTileX;
     const long long gy = (p.ny - 2 + W - 3) / (W - 2);
     const int nzf = p.nz - 2;
     int sms = 152;
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // One CTA per SM: pick the number of z chunks that best fills whole waves, charging each
-    // chunk the three extra planes it stages before its first destination plane.
+    // W = 16: one CTA per SM (W = 8: two).  Pick the number of z chunks that best fills whole
+    // waves, charging each chunk the three extra planes it stages before its first destination
+    // plane.
+    sms *= W == kStepWSmall ? 2 : 1;
     double best = -1.0;
     int best_chunk = nzf;
     for (long long gz = 1; gz <= std::max(1, nzf / 8); ++gz) {
@@ -168,17 +172,18 @@ bool tma_capable(const mbcg_params& p, const void* const* f, long long pitch, in
     return get_encode() != nullptr;
 }
 
-int encode_maps(const mbcg_params& p, const void* const* f, long long pitch, int precision, TensorMaps& T) {
+// TMA descriptors of one state for step CTAs of W rows: rhor / rhob boxes kStepRBX x (W+2),
+// the other fields kStepMX x W, one plane deep
+int encode_maps(const mbcg_params& p, const void* const* f, long long pitch, int precision, int W, TensorMaps& T) {
     EncodeFn enc = get_encode();
     if (!enc) return fail(MBCG_E_CUDA, "cuTensorMapEncodeTiled unavailable");
     const int es = elem_bytes(precision);
-    const int W = step_box_rows();
     for (int i = 0; i < NF; ++i) {
         const cuuint64_t dims[3] = {static_cast<cuuint64_t>(p.nx), static_cast<cuuint64_t>(p.ny),
                                     static_cast<cuuint64_t>(p.nz)};
         const cuuint64_t strides[2] = {static_cast<cuuint64_t>(pitch * es),
                                        static_cast<cuuint64_t>(pitch * p.ny * es)};
-        const cuuint32_t box[3] = {static_cast<cuuint32_t>(i < 2 ? step_rb_box_x() : step_m_box_x()),
+        const cuuint32_t box[3] = {static_cast<cuuint32_t>(i < 2 ? kStepRBX : kStepMX),
                                    static_cast<cuuint32_t>(i < 2 ? W + 2 : W), 1u};
         const cuuint32_t estr[3] = {1u, 1u, 1u};
         const CUresult r = enc(&T.m[i], es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3,
@@ -188,6 +193,33 @@ int encode_maps(const mbcg_params& p, const void* const* f, long long pitch, int
         if (r != CUDA_SUCCESS) return fail(MBCG_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(r) + ")");
     }
     return MBCG_OK;
+}
+
+// ---------------------------------------------------------------- tuned shapes
+// Process-wide table of the shapes mbcg_autotune() measured, keyed by everything that changes
+// the kernel's work per node: lattice, storage precision, sizes and feature set.
+struct ShapeKey {
+    int q, precision, nx, ny, nz, features;
+    bool operator<(const ShapeKey& o) const {
+        return std::tie(q, precision, nx, ny, nz, features) < std::tie(o.q, o.precision, o.nx, o.ny, o.nz, o.features);
+    }
+};
+std::mutex g_tune_mu;
+std::map<ShapeKey, std::pair<int, int>> g_tuned;
+
+ShapeKey shape_key(const mbcg_params& p) {
+    StepParams P;
+    fill_physics(p, P);
+    return ShapeKey{p.q, p.precision, p.nx, p.ny, p.nz, features_of(P)};
+}
+
+bool tuned_shape(const mbcg_params& p, int* w, int* zchunk) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(shape_key(p));
+    if (it == g_tuned.end()) return false;
+    *w = it->second.first;
+    *zchunk = it->second.second;
+    return true;
 }
 
 } // namespace
@@ -208,7 +240,8 @@ struct mbcg_case {
     double* diag_result = nullptr;
     int nparts = 0;
     long long steps = 0;
-    int zchunk = 16;
+    int w = kStepW;   // step CTA rows
+    int zchunk = 16;  // destination planes per step CTA
 };
 
 namespace {
@@ -267,7 +300,7 @@ StepParams raw_params(const mbcg_params* p, const mbcg_moments* a, const mbcg_mo
     fill_physics(*p, P);
     P.pitch = b ? b->pitch : a->pitch;
     P.plane = P.pitch * p->ny;
-    P.zchunk = choose_zchunk(*p);
+    P.zchunk = choose_zchunk(*p, kStepW);
     P.step = step;
     P.status = raw_status();
     for (int i = 0; i < NF; ++i) {
@@ -342,7 +375,10 @@ int mbcg_create(const mbcg_params* p, mbcg_case** out) {
         return fail(MBCG_E_NOMEM, "cudaMalloc of the status word failed");
     }
     cudaMemset(c->status, 0, sizeof(int));
-    c->zchunk = choose_zchunk(*p);
+    if (!tuned_shape(*p, &c->w, &c->zchunk)) {
+        c->w = kStepW;
+        c->zchunk = choose_zchunk(*p, c->w);
+    }
     {
         StepParams P = make_params(c, 0, 0);
         c->nparts = diag_partials_needed(P);
@@ -356,7 +392,7 @@ int mbcg_create(const mbcg_params* p, mbcg_case** out) {
              tma_capable(*p, c->fields[1], c->pitch, p->precision);
     if (c->tma) {
         for (int s = 0; s < 2; ++s)
-            if (int rc = encode_maps(*p, c->fields[s], c->pitch, p->precision, c->tm[s])) {
+            if (int rc = encode_maps(*p, c->fields[s], c->pitch, p->precision, c->w, c->tm[s])) {
                 free_case(c);
                 return rc;
             }
@@ -390,7 +426,7 @@ int mbcg_step(mbcg_case* c, int32_t nsteps, mbcg_stream_t s) {
     if (nsteps < 0) return fail(MBCG_E_INVALID, "negative step count");
     for (int n = 0; n < nsteps; ++n) {
         StepParams P = make_params(c, c->cur, c->steps + 1);
-        MBCG_TRY(launch_step(c->p.q, c->p.precision, c->tma, P, c->tm[c->cur], reinterpret_cast<cudaStream_t>(s)),
+        MBCG_TRY(launch_step(c->p.q, c->p.precision, c->tma, c->w, P, c->tm[c->cur], reinterpret_cast<cudaStream_t>(s)),
                  "step kernel");
         c->cur ^= 1;
         c->steps += 1;
@@ -402,7 +438,7 @@ int mbcg_rcs(mbcg_case* c, mbcg_stream_t s) {
     if (!c) return fail(MBCG_E_INVALID, "null case");
     StepParams P = make_params(c, c->cur, c->steps + 1);
     P.do_bc = 0;
-    MBCG_TRY(launch_step(c->p.q, c->p.precision, c->tma, P, c->tm[c->cur], reinterpret_cast<cudaStream_t>(s)),
+    MBCG_TRY(launch_step(c->p.q, c->p.precision, c->tma, c->w, P, c->tm[c->cur], reinterpret_cast<cudaStream_t>(s)),
              "RCS kernel");
     return MBCG_OK;
 }
@@ -548,8 +584,8 @@ int mbcg_rcs_moments(const mbcg_params* p, const mbcg_moments* a, const mbcg_mom
     std::memset(&T, 0, sizeof(T));
     const bool tma = tma_capable(*p, a->f, a->pitch, p->precision);
     if (tma)
-        if (int rc = encode_maps(*p, a->f, a->pitch, p->precision, T)) return rc;
-    MBCG_TRY(launch_step(p->q, p->precision, tma, P, T, reinterpret_cast<cudaStream_t>(s)), "RCS kernel");
+        if (int rc = encode_maps(*p, a->f, a->pitch, p->precision, kStepW, T)) return rc;
+    MBCG_TRY(launch_step(p->q, p->precision, tma, kStepW, P, T, reinterpret_cast<cudaStream_t>(s)), "RCS kernel");
     return MBCG_OK;
 }
 
@@ -569,6 +605,87 @@ int mbcg_init_moments(const mbcg_params* p, const mbcg_moments* a, mbcg_stream_t
     if (int rc = check_view(p, a)) return rc;
     StepParams P = raw_params(p, nullptr, a, 0);
     MBCG_TRY(launch_init(p->precision, P, *p, reinterpret_cast<cudaStream_t>(s)), "initial condition");
+    return MBCG_OK;
+}
+
+int mbcg_get_shape(const mbcg_case* c, int32_t* block_rows, int32_t* zchunk) {
+    if (!c || !block_rows || !zchunk) return fail(MBCG_E_INVALID, "null argument");
+    *block_rows = c->w;
+    *zchunk = c->zchunk;
+    return MBCG_OK;
+}
+
+int mbcg_set_shape(mbcg_case* c, int32_t block_rows, int32_t zchunk) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    if (block_rows != kStepW && block_rows != kStepWSmall) return fail(MBCG_E_INVALID, "block_rows must be 8 or 16");
+    if (zchunk < 1) return fail(MBCG_E_INVALID, "zchunk must be positive");
+    if (block_rows != c->w && c->tma) {
+        TensorMaps t[2];
+        for (int s = 0; s < 2; ++s)
+            if (int rc = encode_maps(c->p, c->fields[s], c->pitch, c->p.precision, block_rows, t[s])) return rc;
+        c->tm[0] = t[0];
+        c->tm[1] = t[1];
+    }
+    c->w = block_rows;
+    c->zchunk = std::min<int>(zchunk, c->p.nz - 2);
+    return MBCG_OK;
+}
+
+// Times the step for each candidate shape on this case and keeps the fastest.  Every timed
+// launch reads the current state and writes the other one (the state a step would overwrite
+// anyway), so the current state is unchanged.
+int mbcg_autotune(mbcg_case* c, int32_t repeats, double* best_ms, mbcg_stream_t s) {
+    if (!c) return fail(MBCG_E_INVALID, "null case");
+    if (repeats < 1) repeats = 3;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+    const int nzf = c->p.nz - 2;
+    std::vector<std::pair<int, int>> cands;
+    for (int w : {kStepW, kStepWSmall}) {
+        std::vector<int> zs = {choose_zchunk(c->p, w), 4, 8, 16, 32, 64, nzf};
+        for (int z : zs) {
+            z = std::max(1, std::min(z, nzf));
+            if (std::find(cands.begin(), cands.end(), std::make_pair(w, z)) == cands.end()) cands.emplace_back(w, z);
+        }
+    }
+    cudaEvent_t e0, e1;
+    MBCG_TRY(cudaEventCreate(&e0), "event");
+    MBCG_TRY(cudaEventCreate(&e1), "event");
+    double best = 1e300;
+    std::pair<int, int> pick(c->w, c->zchunk);
+    int rc = MBCG_OK;
+    for (const auto& cand : cands) {
+        TensorMaps T;
+        std::memset(&T, 0, sizeof(T));
+        if (c->tma && (rc = encode_maps(c->p, c->fields[c->cur], c->pitch, c->p.precision, cand.first, T))) break;
+        StepParams P = make_params(c, c->cur, c->steps + 1);
+        P.zchunk = cand.second;
+        cudaError_t e = launch_step(c->p.q, c->p.precision, c->tma, cand.first, P, T, st);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+        for (int r = 0; r < repeats && e == cudaSuccess; ++r)
+            e = launch_step(c->p.q, c->p.precision, c->tma, cand.first, P, T, st);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "autotune");
+            break;
+        }
+        const double per = ms / repeats;
+        if (per < best) {
+            best = per;
+            pick = cand;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (int r2 = mbcg_set_shape(c, pick.first, pick.second)) return r2;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tuned[shape_key(c->p)] = pick;
+    }
+    if (best_ms) *best_ms = best;
     return MBCG_OK;
 }
 

@@ -11,19 +11,29 @@
 
 namespace mbcg {
 
-constexpr int kStepW = 16; // warps (rows) per step CTA: 14 destination rows + 2 halo rows
+// Step CTA shapes: W warps = W source rows (W-2 destination rows plus a halo row on each
+// side) by 32 lanes (30 destination columns plus halo).  The plain step is built for both.
+constexpr int kStepW = 16;     // default
+constexpr int kStepWSmall = 8; // two CTAs per SM
+constexpr int kStepTileX = 30; // destination columns per tile
+constexpr int kStepRBX = 48;   // staged width of the rhor / rhob boxes
+constexpr int kStepMX = 40;    // staged width of the other nine boxes
 
 struct TensorMaps {
     CUtensorMap m[NF];
 };
 
-// fused step (mbcg_step.cu)
-cudaError_t launch_step(int q, int precision, bool tma, const StepParams& P, const TensorMaps& T, cudaStream_t s);
-int step_smem_bytes(int precision);
-int step_box_rows();
-int step_tile_x();
-int step_rb_box_x();
-int step_m_box_x();
+// fused step (mbcg_step.cu; instantiations in mbcg_step_q{19,27}_{f32,f16,bf16}.cu)
+cudaError_t launch_step(int q, int precision, bool tma, int w, const StepParams& P, const TensorMaps& T,
+                        cudaStream_t s);
+cudaError_t launch_step_q19_f32(bool tma, int w, const StepParams& P, const TensorMaps& T, cudaStream_t s);
+cudaError_t launch_step_q19_f16(bool tma, int w, const StepParams& P, const TensorMaps& T, cudaStream_t s);
+cudaError_t launch_step_q19_bf16(bool tma, int w, const StepParams& P, const TensorMaps& T, cudaStream_t s);
+cudaError_t launch_step_q27_f32(bool tma, int w, const StepParams& P, const TensorMaps& T, cudaStream_t s);
+cudaError_t launch_step_q27_f16(bool tma, int w, const StepParams& P, const TensorMaps& T, cudaStream_t s);
+cudaError_t launch_step_q27_bf16(bool tma, int w, const StepParams& P, const TensorMaps& T, cudaStream_t s);
+int step_smem_bytes(int precision, int w);
+inline int step_tile_rows(int w) { return w - 2; }
 
 // boundary functors, initial conditions, diagnostics, layout conversion (mbcg_aux.cu)
 cudaError_t launch_bc(int precision, const StepParams& P, cudaStream_t s);

@@ -11,6 +11,8 @@
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 
+#include "mbcg.h"
+
 namespace mbcg {
 
 #define MBCG_HD __host__ __device__ __forceinline__
@@ -126,6 +128,19 @@ struct StepParams {
     const void* a[NF];  // current state
     void* b[NF];        // next state
 };
+
+// Optional parts of the step a lattice needs: bounce-back walls, a body force or density-ratio
+// rest term, an inlet/outlet axis.  Kernels are instantiated per feature set.
+constexpr int F_WALL = 1, F_FORCE = 2, F_INOUT = 4, F_ALL = 7;
+
+MBCG_HD int features_of(const StepParams& P) {
+    int f = 0;
+    for (int a = 0; a < 3; ++a)
+        if (P.bc[a] == MBCG_BC_WALL) f |= F_WALL;
+    if (P.forced || P.ratio) f |= F_FORCE;
+    if (P.inout_axis >= 0) f |= F_INOUT;
+    return f;
+}
 
 // Counter-based inlet-noise generator: SplitMix64 finaliser (Steele, Lea & Flood 2014) on
 // (seed, step) and then on (dense node index, component).  Uniform in [-1, 1), 24 bits.

@@ -1,1046 +1,28 @@
-// mbcg_step.cu -- fused moment-based colour-gradient time step for sm_103a (GB300).
-//
-// One kernel launch = one time step of the reference's main loop (main.cu:41-45):
-//   RCS (lbm.cuh:20-262)  +  jet inlet/outlet functors (kernels.cu:102-114)  [+ swap by the host]
-//
-// Formulation.  The reference pulls, for every destination node and direction i, the post-
-// collision population of the source node x - c_i and rebuilds it from the source's 11
-// moments (feq + oms*fneqr, Omega2 and recolouring at interfaces).  Every one of those
-// populations is a polynomial in c_i whose coefficients depend only on the source node, so
-// here each source node is visited once:
-//   1. its coefficient tensor p_abc (monomials cx^a cy^b cz^c, a,b,c <= 2; 17 non-zero) is
-//      built from the moments (equilibrium, regularised non-equilibrium, Guo force,
-//      density-ratio rest term, Omega2), plus the rest-population correction r0;
-//   2. a separable inverse transform over x, y, z evaluates all Q populations g_i = w_i V(c_i)
-//      (+ r0 at i = 0); red populations are fr_i = aR g_i + Delta_i (recolouring);
-//   3. populations are streamed and projected onto the destination's moments by the
-//      separable forward transform, one axis at a time:
-//        z: the CTA marches along z; class cz of source plane k feeds destination plane k+cz,
-//        x: warp lanes are consecutive x nodes; neighbours exchange by __shfl_up/down_sync,
-//        y: warps are consecutive y rows; neighbours exchange through shared memory.
-// The colour gradient F (forces.cuh:20-60) is evaluated once per interface source node from a
-// 3-plane ring of psi = (rhor - rhob)/rho kept in shared memory.
-//
-// Tiling.  A CTA is 32 lanes (x) x W warps (y).  Lanes 0 and 31 and warps 0 and W-1 are
-// halo sources; the CTA writes the 30 x (W-2) destination columns in between, for a chunk of
-// zchunk planes.  Each source plane arrives in shared memory through TMA
-// (cp.async.bulk.tensor.3d, one box per field, 4-slot ring tracked by mbarriers).  Periodic
-// axes are wrapped by mapping coordinates (bounds.cuh:34-77); the rare nodes whose data is a
-// periodic image outside the staged box are read from global memory directly.
-//
-// Boundary kinds: periodic; inlet/outlet (the reference's ghost-source branch,
-// lbm.cuh:79-151, plus the inlet and outlet functors fused into the store of the first and
-// last fluid layer); wall (halfway bounce-back).
-#include <cuda.h>
-#include <cuda_runtime.h>
-#include <cstdint>
-#include <cstdio>
-#include <type_traits>
-
-#include "mbcg_lattice.cuh"
-#include "mbcg_internal.h"
+// mbcg_step.cu -- dispatch of the plain fused step to its (lattice, storage) instantiation.
+#include "mbcg_step.cuh"
 
 namespace mbcg {
 
-namespace {
-
-constexpr int kTX = 30;    // destination columns per CTA
-constexpr int kRBX = 48;   // staged width of rhor/rhob rows (34 needed + 16-byte alignment slack)
-constexpr int kMX = 40;    // staged width of the other 9 fields (32 needed + slack)
-constexpr int kPSX = 34;   // psi ring width (32 sources + 1 on each side)
-constexpr int kNSTAGE = 3; // planes staged: k, k+1 and the one in flight, k+2
-constexpr unsigned kFull = 0xffffffffu;
-
-constexpr int align128(int b) { return (b + 127) / 128 * 128; }
-
-template <typename S, int W>
-struct Geo {
-    static constexpr int RBY = W + 2;
-    static constexpr int MY = W;
-    static constexpr int rb_field = align128(RBY * kRBX * (int)sizeof(S));
-    static constexpr int m_field = align128(MY * kMX * (int)sizeof(S));
-    static constexpr int stage = 2 * rb_field + 9 * m_field;
-    static constexpr int tx = 2 * RBY * kRBX * (int)sizeof(S) + 9 * MY * kMX * (int)sizeof(S);
-    static constexpr int psi_plane = RBY * kPSX;           // floats
-    static constexpr int psi = 3 * psi_plane * 4;          // bytes
-    static constexpr int xbuf_floats = 3 * 2 * 4 * W * 32; // [class][slot][comp][row][lane]
-    static constexpr int xbuf = xbuf_floats * 4;
-    static constexpr int off_psi = kNSTAGE * stage;
-    static constexpr int off_xbuf = off_psi + psi;
-    static constexpr int off_bar = off_xbuf + xbuf;
-    static constexpr int smem = off_bar + kNSTAGE * 8 + 128;
-};
-
-// ------------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait: gives up after ~limit clock cycles instead of spinning forever.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > limit) return false;
-    }
-    return true;
-}
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-        : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ int floor8(int v) { return v & ~7; }
-
-// ------------------------------------------------------------------ coordinate roles
-enum Role : int { R_FLUID = 0, R_IMAGE = 1, R_GHOST = 2, R_WALL = 3, R_OUT = 4 };
-
-__device__ __forceinline__ int axis_role(const StepParams& P, int a, int p, int n) {
-    if (p < 0 || p > n - 1) return R_OUT;
-    if (p == 0 || p == n - 1) {
-        const int k = P.bc[a];
-        return k == MBCG_BC_PERIODIC ? R_IMAGE : (k == MBCG_BC_INOUT ? R_GHOST : R_WALL);
-    }
-    return R_FLUID;
-}
-__device__ __forceinline__ int data_coord(const StepParams& P, int a, int p, int n) {
-    return (P.bc[a] == MBCG_BC_PERIODIC) ? periodic_image(p, n) : min(max(p, 0), n - 1);
-}
-// neighbour rule of the colour gradient (forces.cuh:28-31, mathUtilities.cuh:25-33)
-__device__ __forceinline__ int psi_coord(const StepParams& P, int a, int p, int n) {
-    const int k = P.bc[a];
-    if (k == MBCG_BC_PERIODIC) return periodic_image(p, n);
-    if (k == MBCG_BC_INOUT) return p >= n - 1 ? n - 2 : max(p, 0);
-    return min(max(p, 1), n - 2);
-}
-
-// ------------------------------------------------------------------ state access
-template <typename S>
-struct Node {
-    float rr, rb, ux, uy, uz, pxx, pxy, pyy, pyz, pzz, pxz;
-};
-
-template <typename S>
-__device__ __forceinline__ float psi_of(const StepParams& P, S s0, S s1) {
-    if constexpr (std::is_same<S, float>::value) {
-        const float r = Codec<S>::to_f(s0), b = Codec<S>::to_f(s1);
-        return __fdividef(r - b, r + b);
-    } else {
-        (void)P;
-        (void)s0;
-        return Codec<S>::to_f(s1);
-    }
-}
-
-// psi from the two stored slots already widened to float
-template <typename S>
-__device__ __forceinline__ float psi_of_slots(float v0, float v1) {
-    if constexpr (std::is_same<S, float>::value) return __fdividef(v0 - v1, v0 + v1);
-    else return v1;
-}
-
-// decode the 11 stored slots into the reference's moments
-template <typename S>
-__device__ __forceinline__ void decode(const StepParams& P, const float (&v)[NF], Node<S>& n) {
-    if constexpr (sizeof(S) == 4) {
-        n.rr = v[0]; n.rb = v[1]; n.ux = v[2]; n.uy = v[3]; n.uz = v[4];
-        n.pxx = v[5]; n.pxy = v[6]; n.pyy = v[7]; n.pyz = v[8]; n.pzz = v[9]; n.pxz = v[10];
-    } else {
-        const float phi = v[1];
-        const float rho = P.rho_mean + phi * P.rho_half_diff + P.rho_scale * v[0];
-        n.rr = 0.5f * rho * (1.0f + phi);
-        n.rb = 0.5f * rho * (1.0f - phi);
-        n.ux = P.u_ref * v[2]; n.uy = P.u_ref * v[3]; n.uz = P.u_ref * v[4];
-        n.pxx = P.pi_scale * v[5]; n.pxy = P.pi_scale * v[6]; n.pyy = P.pi_scale * v[7];
-        n.pyz = P.pi_scale * v[8]; n.pzz = P.pi_scale * v[9]; n.pxz = P.pi_scale * v[10];
-    }
-}
-
-template <typename S>
-__device__ __forceinline__ void encode(const StepParams& P, float rr, float rb, const float (&u)[3],
-                                       const float (&pi)[6], S (&out)[NF]) {
-    if constexpr (sizeof(S) == 4) {
-        out[0] = rr; out[1] = rb; out[2] = u[0]; out[3] = u[1]; out[4] = u[2];
-        for (int i = 0; i < 6; ++i) out[5 + i] = pi[i];
-    } else {
-        const float rho = rr + rb;
-        const float phi = (rr - rb) / rho;
-        out[0] = Codec<S>::from_f((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale);
-        out[1] = Codec<S>::from_f(phi);
-        for (int i = 0; i < 3; ++i) out[2 + i] = Codec<S>::from_f(u[i] * P.inv_u_ref);
-        for (int i = 0; i < 6; ++i) out[5 + i] = Codec<S>::from_f(pi[i] * P.inv_pi_scale);
-    }
-}
-
-template <typename S>
-__device__ __forceinline__ void store_node(const StepParams& P, long long o, const S (&v)[NF]) {
-#pragma unroll
-    for (int f = 0; f < NF; ++f) static_cast<S*>(P.b[f])[o] = v[f];
-}
-
-template <typename S>
-__device__ __forceinline__ void load_global(const StepParams& P, long long o, float (&v)[NF]) {
-#pragma unroll
-    for (int f = 0; f < NF; ++f) v[f] = Codec<S>::to_f(static_cast<const S*>(P.a[f])[o]);
-}
-
-// ------------------------------------------------------------------ coefficient tensor
-struct Coef {
-    float p000, p100, p010, p001, p200, p020, p002, p110, p101, p011;
-    float p210, p201, p120, p102, p021, p012, p111, r0;
-};
-
-// Equilibrium (pdf.cuh:16-36) at (rho, u) + oms * regularised non-equilibrium (pdf.cuh:38-79)
-// from (Pi, v) + 1/2 Guo force (pdf.cuh:94-136) + density-ratio rest term, as the
-// coefficients of a polynomial in c (w_i factored out).
-__device__ __forceinline__ void build_coef(const StepParams& P, Coef& c, float rho, float rr, float rb, float ux,
-                                           float uy, float uz, float vx, float vy, float vz, float pxx, float pxy,
-                                           float pyy, float pyz, float pzz, float pxz) {
-    const float oms = P.oms;
-    const float usq = ux * ux + uy * uy + uz * uz;
-    const float rux = rho * ux, ruy = rho * uy, ruz = rho * uz;
-    const float t1 = 3.0f - 4.5f * usq;
-    const float a3xxy = pxx * vy + 2.0f * pxy * vx;
-    const float a3xxz = pxx * vz + 2.0f * pxz * vx;
-    const float a3xyy = pyy * vx + 2.0f * pxy * vy;
-    const float a3xzz = pzz * vx + 2.0f * pxz * vz;
-    const float a3yyz = pyy * vz + 2.0f * pyz * vy;
-    const float a3yzz = pzz * vy + 2.0f * pyz * vz;
-    const float a3xyz = pxy * vz + pxz * vy + pyz * vx;
-    const float o45 = 4.5f * oms, o9 = 9.0f * oms, o135 = 13.5f * oms;
-    // p000 holds only the small isotropic part; rho itself is added to every direction last
-    // (see emit), so the rounding of rho + small treats rest and moving populations alike
-    c.p000 = -1.5f * (rho * usq + oms * (pxx + pyy + pzz));
-    c.p100 = rux * t1 + 4.5f * rux * ux * ux - o45 * (a3xyy + a3xzz);
-    c.p010 = ruy * t1 + 4.5f * ruy * uy * uy - o45 * (a3xxy + a3yzz);
-    c.p001 = ruz * t1 + 4.5f * ruz * uz * uz - o45 * (a3xxz + a3yyz);
-    c.p200 = 4.5f * rux * ux + o45 * pxx;
-    c.p020 = 4.5f * ruy * uy + o45 * pyy;
-    c.p002 = 4.5f * ruz * uz + o45 * pzz;
-    c.p110 = 9.0f * rux * uy + o9 * pxy;
-    c.p101 = 9.0f * rux * uz + o9 * pxz;
-    c.p011 = 9.0f * ruy * uz + o9 * pyz;
-    c.p210 = 13.5f * rux * ux * uy + o135 * a3xxy;
-    c.p201 = 13.5f * rux * ux * uz + o135 * a3xxz;
-    c.p120 = 13.5f * rux * uy * uy + o135 * a3xyy;
-    c.p102 = 13.5f * rux * uz * uz + o135 * a3xzz;
-    c.p021 = 13.5f * ruy * uy * uz + o135 * a3yyz;
-    c.p012 = 13.5f * ruy * uz * uz + o135 * a3yzz;
-    c.p111 = 27.0f * rux * uy * uz + 2.0f * o135 * a3xyz;
-    c.r0 = 0.0f;
-    if (P.forced) {
-        const float Fx = rho * P.g[0], Fy = rho * P.g[1], Fz = rho * P.g[2];
-        const float Gxxy = Fx * ux * uy + 0.5f * Fy * ux * ux;
-        const float Gxxz = Fx * ux * uz + 0.5f * Fz * ux * ux;
-        const float Gxyy = Fy * ux * uy + 0.5f * Fx * uy * uy;
-        const float Gxzz = Fz * ux * uz + 0.5f * Fx * uz * uz;
-        const float Gyyz = Fy * uy * uz + 0.5f * Fz * uy * uy;
-        const float Gyzz = Fz * uy * uz + 0.5f * Fy * uz * uz;
-        const float Gxyz = Fx * uy * uz + Fy * ux * uz + Fz * ux * uy;
-        c.p000 -= 1.5f * (Fx * ux + Fy * uy + Fz * uz);
-        c.p100 += 1.5f * Fx - 4.5f * (Gxyy + Gxzz);
-        c.p010 += 1.5f * Fy - 4.5f * (Gxxy + Gyzz);
-        c.p001 += 1.5f * Fz - 4.5f * (Gxxz + Gyyz);
-        c.p200 += 4.5f * Fx * ux;
-        c.p020 += 4.5f * Fy * uy;
-        c.p002 += 4.5f * Fz * uz;
-        c.p110 += 4.5f * (Fx * uy + Fy * ux);
-        c.p101 += 4.5f * (Fx * uz + Fz * ux);
-        c.p011 += 4.5f * (Fy * uz + Fz * uy);
-        c.p210 += 13.5f * Gxxy;
-        c.p201 += 13.5f * Gxxz;
-        c.p120 += 13.5f * Gxyy;
-        c.p102 += 13.5f * Gxzz;
-        c.p021 += 13.5f * Gyyz;
-        c.p012 += 13.5f * Gyzz;
-        c.p111 += 13.5f * Gxyz;
-    }
-    if (P.ratio) {
-        const float K = rr * P.kappa_r + rb * P.kappa_b;
-        c.p000 += K;
-        c.r0 -= K;
-    }
-}
-
-// ------------------------------------------------------------------ accumulators
-struct Acc {
-    float rho, jx, jy, jz, xx, xy, yy, yz, zz, xz, red;
-    __device__ __forceinline__ void zero() { rho = jx = jy = jz = xx = xy = yy = yz = zz = xz = red = 0.0f; }
-};
-
-// add one population of velocity (ex, ey, ez) to a destination's moment sums
-__device__ __forceinline__ void add_pop(Acc& a, float g, float r, int ex, int ey, int ez) {
-    a.rho += g;
-    a.red += r;
-    if (ex) { a.jx += ex * g; a.xx += g; }
-    if (ey) { a.jy += ey * g; a.yy += g; }
-    if (ez) { a.jz += ez * g; a.zz += g; }
-    if (ex && ey) a.xy += ex * ey * g;
-    if (ey && ez) a.yz += ey * ez * g;
-    if (ex && ez) a.xz += ex * ez * g;
-}
-
-// ------------------------------------------------------------------ the kernel
-// fast reciprocal (MUFU-based, <= 2 ulp); the colour fraction of a pure node stays exact
-__device__ __forceinline__ float fast_rcp(float v) { return __fdividef(1.0f, v); }
-
-// Store one node at (x, y, z); on periodic x / y axes the first and last fluid layers are also
-// written to their image in the opposite ghost layer, so the next step reads every source
-// (including wrapped ones) from the staged box (bounds.cuh:34-77 wraps on read instead).
-template <typename S>
-__device__ __forceinline__ void finalize_store(const StepParams& P, int x, int y, int z, float rr, float rb,
-                                               float ux, float uy, float uz, const float (&pi)[6]) {
-    const float u[3] = {ux, uy, uz};
-    S out[NF];
-    encode<S>(P, rr, rb, u, pi, out);
-    const long long zo = static_cast<long long>(z) * P.plane;
-    store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + x, out);
-    if (P.ghost_images) {
-        const int ix = P.bc[0] == MBCG_BC_PERIODIC ? (x == 1 ? P.nx - 1 : (x == P.nx - 2 ? 0 : -1)) : -1;
-        const int iy = P.bc[1] == MBCG_BC_PERIODIC ? (y == 1 ? P.ny - 1 : (y == P.ny - 2 ? 0 : -1)) : -1;
-        if (ix >= 0) store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + ix, out);
-        if (iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + x, out);
-        if (ix >= 0 && iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + ix, out);
-    }
-}
-
-template <int Q, typename S, int W, bool kTMA>
-__global__ void __launch_bounds__(32 * W, 1) step_kernel(const __grid_constant__ StepParams P,
-                                                         const __grid_constant__ TensorMaps T) {
-    using G = Geo<S, W>;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    // TMA destinations need 128-byte alignment: round the dynamic base up (G::smem has slack)
-    unsigned char* smem =
-        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float* psi_ring = reinterpret_cast<float*>(smem + G::off_psi);
-    float* xbuf = reinterpret_cast<float*>(smem + G::off_xbuf);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G::off_bar);
-
-    const int lane = threadIdx.x;
-    const int w = threadIdx.y;
-    const int tid = w * 32 + lane;
-    const int nx = P.nx, ny = P.ny, nz = P.nz;
-
-    const int xb = kTX * blockIdx.x;     // source column of lane 0
-    const int yb = (W - 2) * blockIdx.y; // source row of warp 0
-    const int xs = xb + lane, ys = yb + w;
-    const int zd0 = 1 + P.zchunk * blockIdx.z;
-    const int zd1 = min(zd0 + P.zchunk, nz - 1);
-    const int kfirst = zd0 - 2;
-
-    const int xr0 = floor8(xb - 1); // first staged column of rhor/rhob
-    const int xm0 = floor8(xb);     // first staged column of the other fields
-    const int offRB = xb - xr0;
-    const int offM = xb - xm0;
-    const int bR = (w + 1) * kRBX + lane + offRB; // this node in the rhor/rhob boxes
-    const int bM = w * kMX + lane + offM;         // this node in the other boxes
-
-    const bool dest_thread = lane >= 1 && lane <= kTX && w >= 1 && w <= W - 2 && xs <= nx - 2 && ys <= ny - 2;
-    const int rx = axis_role(P, 0, xs, nx);
-    const int ry = axis_role(P, 1, ys, ny);
-    const bool col_in_box = (rx != R_IMAGE || P.ghost_images) && (ry != R_IMAGE || P.ghost_images);
-    const long long gxy = static_cast<long long>(data_coord(P, 1, ys, ny)) * P.pitch + data_coord(P, 0, xs, nx);
-    const int ia = P.inout_axis;
-
-    // psi fill: each thread owns <= kPsiPer ring elements; their mapping never changes along z.
-    // Each element reads the staged box at the node whose stored value equals psi there (the
-    // periodic ghost frame holds images), or, for the periodic images two layers out that the
-    // box cannot hold, a global load issued one plane ahead into registers.
-    constexpr int kPsiPer = (G::psi_plane + 32 * W - 1) / (32 * W);
-    int psi_box[kPsiPer];      // box index, -1: prefetched global load, -2: no element
-    long long psi_g[kPsiPer];  // mapped (x, y) offset in global memory
-    float pf0[kPsiPer], pf1[kPsiPer];
-#pragma unroll
-    for (int j = 0; j < kPsiPer; ++j) {
-        const int e = tid + j * 32 * W;
-        psi_box[j] = -2;
-        psi_g[j] = 0;
-        pf0[j] = pf1[j] = 0.0f;
-        if (e < G::psi_plane) {
-            const int r = e / kPSX, c = e % kPSX;
-            const int gx = xb - 1 + c, gy = yb - 1 + r;
-            const int mx = psi_coord(P, 0, gx, nx), my = psi_coord(P, 1, gy, ny);
-            const bool px = P.bc[0] == MBCG_BC_PERIODIC, py = P.bc[1] == MBCG_BC_PERIODIC;
-            const int dx = (px && P.ghost_images && gx >= 0 && gx <= nx - 1) ? gx : mx;
-            const int dy = (py && P.ghost_images && gy >= 0 && gy <= ny - 1) ? gy : my;
-            const int bc_ = dx - xr0, br_ = dy - (yb - 1);
-            psi_box[j] = (bc_ >= 0 && bc_ < kRBX && br_ >= 0 && br_ < G::RBY) ? br_ * kRBX + bc_ : -1;
-            psi_g[j] = static_cast<long long>(my) * P.pitch + mx;
+cudaError_t launch_step(int q, int precision, bool tma, int w, const StepParams& P, const TensorMaps& T,
+                        cudaStream_t s) {
+    if (w != kStepW && w != kStepWSmall) return cudaErrorInvalidValue;
+    if (q == 27) {
+        switch (precision) {
+        case MBCG_FP16: return launch_step_q27_f16(tma, w, P, T, s);
+        case MBCG_BF16: return launch_step_q27_bf16(tma, w, P, T, s);
+        default: return launch_step_q27_f32(tma, w, P, T, s);
         }
     }
-
-    auto slot_of = [&](int k) -> int { return (k - kfirst) % kNSTAGE; };
-    auto stage_ptr = [&](int k) -> unsigned char* { return smem + slot_of(k) * G::stage; };
-    auto rb_box = [&](unsigned char* st, int f) -> S* { return reinterpret_cast<S*>(st + f * G::rb_field); };
-    auto m_box = [&](unsigned char* st, int f) -> S* {
-        return reinterpret_cast<S*>(st + 2 * G::rb_field + (f - 2) * G::m_field);
-    };
-    auto zload = [&](int k) -> int { return data_coord(P, 2, k, nz); };
-
-    // ---- stage loader -------------------------------------------------------------
-    auto issue = [&](int k) {
-        unsigned char* st = stage_ptr(k);
-        const int kz = zload(k);
-        if constexpr (kTMA) {
-            if (tid == 0) {
-                uint64_t* bar = &bars[slot_of(k)];
-                fence_proxy_async();
-                mbar_expect_tx(bar, G::tx);
-                tma_load_3d(rb_box(st, 0), &T.m[0], xr0, yb - 1, kz, bar);
-                tma_load_3d(rb_box(st, 1), &T.m[1], xr0, yb - 1, kz, bar);
-#pragma unroll
-                for (int f = 2; f < NF; ++f) tma_load_3d(m_box(st, f), &T.m[f], xm0, yb, kz, bar);
-            }
-        } else {
-            // plain-load path for layouts TMA cannot describe (row pitch not 16-byte aligned)
-            const long long zo = static_cast<long long>(kz) * P.plane;
-            for (int e = tid; e < 2 * G::RBY * kRBX; e += 32 * W) {
-                const int f = e / (G::RBY * kRBX), r = (e / kRBX) % G::RBY, c = e % kRBX;
-                const int gx = xr0 + c, gy = yb - 1 + r;
-                S v = Codec<S>::from_f(0.0f);
-                if (gx >= 0 && gx < nx && gy >= 0 && gy < ny)
-                    v = static_cast<const S*>(P.a[f])[zo + gy * P.pitch + gx];
-                rb_box(st, f)[r * kRBX + c] = v;
-            }
-            for (int e = tid; e < 9 * G::MY * kMX; e += 32 * W) {
-                const int f = 2 + e / (G::MY * kMX), r = (e / kMX) % G::MY, c = e % kMX;
-                const int gx = xm0 + c, gy = yb + r;
-                S v = Codec<S>::from_f(0.0f);
-                if (gx >= 0 && gx < nx && gy >= 0 && gy < ny)
-                    v = static_cast<const S*>(P.a[f])[zo + gy * P.pitch + gx];
-                m_box(st, f)[r * kMX + c] = v;
-            }
-        }
-    };
-    constexpr long long kWaitLimit = 4000000000LL; // ~2 s at 2 GHz
-    auto wait_stage = [&](int k) -> bool {
-        if constexpr (kTMA) {
-            const int j = k - kfirst;
-            return mbar_wait_bounded(&bars[j % kNSTAGE], static_cast<uint32_t>((j / kNSTAGE) & 1), kWaitLimit);
-        } else {
-            return true;
-        }
-    };
-    // on a failed wait: flag it, drain the copies still in flight (bounded) and leave
-    auto bail = [&](int k_failed, int k_issued) {
-        if (tid == 0 && P.status) atomicOr(P.status, 1);
-        if constexpr (kTMA) {
-            for (int k = k_failed + 1; k <= k_issued; ++k) {
-                const int j = k - kfirst;
-                mbar_wait_bounded(&bars[j % kNSTAGE], static_cast<uint32_t>((j / kNSTAGE) & 1), kWaitLimit / 4);
-            }
-        }
-    };
-
-    // ---- psi ring: psi = (rhor - rhob)/rho (mathUtilities.cuh:12-19) of plane k over
-    // columns xb-1..xb+32 and rows yb-1..yb+W, colour-gradient neighbour rule applied
-    auto prefetch_psi = [&](int k) {
-        const long long zo = static_cast<long long>(psi_coord(P, 2, k, nz)) * P.plane;
-#pragma unroll
-        for (int j = 0; j < kPsiPer; ++j)
-            if (psi_box[j] == -1) {
-                pf0[j] = Codec<S>::to_f(static_cast<const S*>(P.a[0])[zo + psi_g[j]]);
-                pf1[j] = Codec<S>::to_f(static_cast<const S*>(P.a[1])[zo + psi_g[j]]);
-            }
-    };
-    auto fill_psi = [&](int k, bool prefetched) {
-        float* ring = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
-        const int mz = psi_coord(P, 2, k, nz);
-        const bool plane_in_box = (mz == zload(k));
-        const long long zo = static_cast<long long>(mz) * P.plane;
-        unsigned char* st = stage_ptr(k);
-        const S* r0b = rb_box(st, 0);
-        const S* r1b = rb_box(st, 1);
-#pragma unroll
-        for (int j = 0; j < kPsiPer; ++j) {
-            if (psi_box[j] == -2) continue;
-            float v;
-            if (plane_in_box && psi_box[j] >= 0) {
-                v = psi_of<S>(P, r0b[psi_box[j]], r1b[psi_box[j]]);
-            } else if (prefetched && psi_box[j] == -1) {
-                v = psi_of_slots<S>(pf0[j], pf1[j]);
-            } else {
-                const long long o = zo + psi_g[j];
-                v = psi_of<S>(P, static_cast<const S*>(P.a[0])[o], static_cast<const S*>(P.a[1])[o]);
-            }
-            ring[tid + j * 32 * W] = v;
-        }
-    };
-
-    // ---- set-up ------------------------------------------------------------------
-    if constexpr (kTMA) {
-        if (tid == 0) {
-            for (int s = 0; s < kNSTAGE; ++s) mbar_init(&bars[s], 1);
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        }
-        __syncthreads();
-    }
-    int k_issued = kfirst + kNSTAGE - 1;
-    for (int k = kfirst; k <= k_issued; ++k) issue(k);
-    if constexpr (!kTMA) __syncthreads();
-    {
-        const bool ok = wait_stage(kfirst) && wait_stage(kfirst + 1);
-        if (__syncthreads_or(!ok)) {
-            bail(kfirst - 1, k_issued);
-            return;
-        }
-    }
-    fill_psi(kfirst, false);
-    fill_psi(kfirst + 1, false);
-    prefetch_psi(kfirst + 2);
-
-    Acc accP, accC, accN; // destination planes k-1, k, k+1
-    accP.zero();
-    accC.zero();
-    accN.zero();
-
-    constexpr float w0 = Stencil<Q>::wk(0);
-    constexpr float cs2 = 1.0f / 3.0f;
-    float* xb_self = xbuf + w * 32 + lane;
-
-    for (int k = zd0 - 1; k <= zd1; ++k) {
-        // (1) psi of plane k+1
-        {
-            const bool ok = wait_stage(k + 1);
-            if (__syncthreads_or(!ok)) {
-                bail(k, k_issued);
-                return;
-            }
-        }
-        fill_psi(k + 1, true);
-        if (k + 2 <= zd1 + 1) prefetch_psi(k + 2);
-        __syncthreads();
-        // (2) prefetch plane k+2 into the slot plane k-1 used
-        if (k + 2 <= zd1 + 1 && k + 2 > k_issued) {
-            issue(k + 2);
-            k_issued = k + 2;
-        }
-
-        // (3) this thread's source node at plane k
-        const int rz = axis_role(P, 2, k, nz);
-        int role = R_FLUID;
-        if (rx == R_OUT || ry == R_OUT || rz == R_OUT) role = R_OUT;
-        else if (rx == R_WALL || ry == R_WALL || rz == R_WALL) role = R_WALL;
-        else if (rx == R_GHOST || ry == R_GHOST || rz == R_GHOST) role = R_GHOST;
-        const bool active = (role == R_FLUID || role == R_GHOST);
-
-        unsigned char* st = stage_ptr(k);
-        const int kz = zload(k);
-        const long long kzo = static_cast<long long>(kz) * P.plane;
-        Node<S> nd{};
-        Node<S> fn{}; // first-fluid node of a ghost source (lbm.cuh:85-89)
-        if (active) {
-            float v[NF];
-            if (col_in_box) {
-                v[0] = Codec<S>::to_f(rb_box(st, 0)[bR]);
-                v[1] = Codec<S>::to_f(rb_box(st, 1)[bR]);
-#pragma unroll
-                for (int f = 2; f < NF; ++f) v[f] = Codec<S>::to_f(m_box(st, f)[bM]);
-            } else {
-                load_global<S>(P, kzo + gxy, v);
-            }
-            decode<S>(P, v, nd);
-            if (role == R_GHOST) {
-                float u[NF];
-                if (rz == R_GHOST) {
-                    // z inlet/outlet ghost: first fluid plane 1 (staged) or nz-2 (global)
-                    if (k == 0 && col_in_box) {
-                        unsigned char* sf = stage_ptr(k + 1);
-#pragma unroll
-                        for (int f = 2; f < NF; ++f) u[f] = Codec<S>::to_f(m_box(sf, f)[bM]);
-                        u[0] = u[1] = 1.0f;
-                    } else {
-                        load_global<S>(P, static_cast<long long>(k == 0 ? 1 : nz - 2) * P.plane + gxy, u);
-                    }
-                } else if (col_in_box) {
-                    const int dx = (rx == R_GHOST) ? (xs == 0 ? 1 : -1) : 0;
-                    const int dy = (ry == R_GHOST) ? (ys == 0 ? 1 : -1) : 0;
-                    const int b2 = bM + dy * kMX + dx;
-#pragma unroll
-                    for (int f = 2; f < NF; ++f) u[f] = Codec<S>::to_f(m_box(st, f)[b2]);
-                    u[0] = u[1] = 1.0f;
-                } else {
-                    const int fx = (rx == R_GHOST) ? (xs == 0 ? 1 : nx - 2) : xs;
-                    const int fy = (ry == R_GHOST) ? (ys == 0 ? 1 : ny - 2) : ys;
-                    load_global<S>(P,
-                                   kzo + static_cast<long long>(data_coord(P, 1, fy, ny)) * P.pitch +
-                                       data_coord(P, 0, fx, nx),
-                                   u);
-                }
-                decode<S>(P, u, fn);
-            }
-        }
-
-        // coefficient tensor and colour split; inactive sources keep all-zero coefficients
-        Coef cf{};
-        float aR = 0.0f, dcoef = 0.0f, Fx = 0.0f, Fy = 0.0f, Fz = 0.0f, omega2_rest = 0.0f;
-        bool iface = false;
-        if (active) {
-            const float rho = nd.rr + nd.rb;
-            const float inv = fast_rcp(rho);
-            // colour fraction as a correctly rounded quotient (one residual correction): a
-            // product with a rounded reciprocal is biased (aR rho - rr averages +2.5e-10 per
-            // mixed node), which would move colour mass the same way every step
-            const float q0 = nd.rr * inv;
-            const float q1 = fmaf(fmaf(-q0, rho, nd.rr), inv, q0);
-            aR = nd.rb == 0.0f ? 1.0f : (nd.rr == 0.0f ? 0.0f : q1);
-            if (role == R_FLUID) {
-                iface = (4.0f * nd.rr * nd.rb * inv * inv) > 1.0e-4f; // lbm.cuh:181,187
-                build_coef(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, nd.ux, nd.uy, nd.uz, nd.pxx, nd.pxy,
-                           nd.pyy, nd.pyz, nd.pzz, nd.pxz);
-            } else {
-                build_coef(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, fn.ux, fn.uy, fn.uz, fn.pxx, fn.pxy,
-                           fn.pyy, fn.pyz, fn.pzz, fn.pxz);
-            }
-        }
-        const bool any_iface = __any_sync(kFull, iface);
-        if (any_iface && iface) {
-            // colour gradient at the source (forces.cuh:20-60) from the psi ring
-            const float* rm = psi_ring + ((k - 1 - kfirst) % 3) * G::psi_plane;
-            const float* r0p = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
-            const float* rp = psi_ring + ((k + 1 - kfirst) % 3) * G::psi_plane;
-            float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-#pragma unroll
-            for (int dz = -1; dz <= 1; ++dz) {
-                const float* ring = dz < 0 ? rm : (dz == 0 ? r0p : rp);
-#pragma unroll
-                for (int dy = -1; dy <= 1; ++dy) {
-#pragma unroll
-                    for (int dx = -1; dx <= 1; ++dx) {
-                        if (dx == 0 && dy == 0 && dz == 0) continue;
-                        if (!Stencil<Q>::has(dx, dy, dz)) continue;
-                        const float ps = ring[(w + 1 + dy) * kPSX + lane + 1 + dx];
-                        const float wp = weight<Q>(dx, dy, dz) * ps;
-                        if (dx) sx += dx * wp;
-                        if (dy) sy += dy * wp;
-                        if (dz) sz += dz * wp;
-                    }
-                }
-            }
-            Fx = 3.0f * sx;
-            Fy = 3.0f * sy;
-            Fz = 3.0f * sz;
-            const float absF = sqrtf(Fx * Fx + Fy * Fy + Fz * Fz);
-            // Omega2 (collisionOperators.cuh:16-25) folded into the coefficients
-            float hA = (P.omega2_conservative && !(absF > 1.0e-4f)) ? 0.0f : 0.5f * P.A * absF;
-            if (absF > 1.0e-4f) {
-                const float ia_ = fast_rcp(absF);
-                const float qf = 0.5f * P.A * ia_;
-                // isotropic part from the same q |F|^2 as the anisotropic part, so Omega2 sums
-                // to zero over the directions in floating point too
-                hA = qf * (Fx * Fx + Fy * Fy + Fz * Fz);
-                cf.p200 += qf * Fx * Fx;
-                cf.p020 += qf * Fy * Fy;
-                cf.p002 += qf * Fz * Fz;
-                cf.p110 += 2.0f * qf * Fx * Fy;
-                cf.p101 += 2.0f * qf * Fx * Fz;
-                cf.p011 += 2.0f * qf * Fy * Fz;
-                // recolouring (collisionOperators.cuh:60-80): beta rr rb / (rho^2 |F|) * feq0, where
-                // the rest equilibrium of moving directions is w rho (w (rho + K) with a density ratio)
-                const float rho = nd.rr + nd.rb;
-                const float feq0 = P.ratio ? rho + nd.rr * P.kappa_r + nd.rb * P.kappa_b : rho;
-                const float irho = fast_rcp(rho);
-                dcoef = P.beta * (nd.rr * nd.rb) * irho * irho * ia_ * feq0;
-            }
-            cf.p000 -= hA;
-            omega2_rest = hA; // rest-population part, -hA (B0 - w0) = +2/3 hA, added below in exact units
-        }
-        const float rho_src = active ? nd.rr + nd.rb : 0.0f;
-
-        // separable inverse transform, x-pass: t_bc(cx) for the monomials cy^b cz^c
-        float t00[3], t10[3], t01[3], t20[3], t02[3], t11[3];
-        {
-            const float a = cf.p000 + cf.p200;
-            t00[1] = cf.p000; t00[2] = a + cf.p100; t00[0] = a - cf.p100;
-            const float b = cf.p010 + cf.p210;
-            t10[1] = cf.p010; t10[2] = b + cf.p110; t10[0] = b - cf.p110;
-            const float d = cf.p001 + cf.p201;
-            t01[1] = cf.p001; t01[2] = d + cf.p101; t01[0] = d - cf.p101;
-            t20[1] = cf.p020; t20[2] = cf.p020 + cf.p120; t20[0] = cf.p020 - cf.p120;
-            t02[1] = cf.p002; t02[2] = cf.p002 + cf.p102; t02[0] = cf.p002 - cf.p102;
-            t11[1] = cf.p011; t11[2] = cf.p011 + cf.p111; t11[0] = cf.p011 - cf.p111;
-        }
-        // Populations are carried scaled by S = 216 (D3Q27) or 36 (D3Q19), where the weights
-        // are small integers that sum to S exactly: float-rounded weights do not sum to 1, and
-        // that error would scale every node's mass each step (about 1.5e-8 per step for D3Q19).
-        // D3Q27 weights are also separable, S w(c) = prod over axes of (4 if c_a = 0 else 1):
-        // populations are carried unweighted and the factors 4 are applied inside the forward
-        // passes.  D3Q19 weights 12, 2, 1 are applied per population.  Each destination
-        // divides its sums by S once, the mass sums with a correctly rounded quotient.
-        constexpr bool kSepW = (Q == 27);
-        const float dk1 = kSepW ? dcoef : 2.0f * dcoef;
-        const float dk2 = dcoef * 0.7071067811865475f;
-        const float dk3 = kSepW ? dcoef * 0.5773502691896258f : 0.0f;
-        // rest-population correction (density-ratio K and the Omega2 rest term), with the Omega2
-        // part in exact units so that Omega2 sums to zero over the directions (B0 - w0 = -2/3
-        // for both lattices)
-        // in value units before the rest weight (64 of 216, or 12 of 36): S r0 / W_0 and
-        // S (w0 - B0) hA / W_0 = (2/3) S hA / W_0, i.e. 3.375 r0 + 2.25 hA or 3 r0 + 2 hA
-        const float rc0 = kSepW ? fmaf(cf.r0, 3.375f, 2.25f * omega2_rest) : fmaf(cf.r0, 3.0f, 2.0f * omega2_rest);
-
-        // wall bounce-back of this node's own populations (destination = this node, plane k)
-        const bool wx0 = P.bc[0] == MBCG_BC_WALL && xs == 1, wx1 = P.bc[0] == MBCG_BC_WALL && xs == nx - 2;
-        const bool wy0 = P.bc[1] == MBCG_BC_WALL && ys == 1, wy1 = P.bc[1] == MBCG_BC_WALL && ys == ny - 2;
-        const bool wz0 = P.bc[2] == MBCG_BC_WALL && k == 1, wz1 = P.bc[2] == MBCG_BC_WALL && k == nz - 2;
-        const bool reflect = role == R_FLUID && dest_thread && (wx0 | wx1 | wy0 | wy1 | wz0 | wz1);
-        const bool any_reflect = __any_sync(kFull, reflect);
-
-        // ---- emit: populations of the rows this warp exports, x streaming, own-row moments,
-        // y exchange.  Halo rows export one population row (cy = +1 for warp 0, -1 for warp W-1).
-        auto emit = [&](auto rowsc) {
-            constexpr int ROWS = decltype(rowsc)::value;
-            float s0[3][3], s1[3][3], e2[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                const float e0 = t00[i] + t20[i];
-                const float e1 = t01[i] + cf.p021;
-                if (ROWS & 2) {
-                    s0[i][1] = t00[i];
-                    s1[i][1] = t01[i];
-                    e2[i][1] = t00[i] + t02[i];
-                }
-                if (ROWS & 4) {
-                    s0[i][2] = e0 + t10[i];
-                    s1[i][2] = e1 + t11[i];
-                    e2[i][2] = s0[i][2] + (t02[i] + cf.p012);
-                }
-                if (ROWS & 1) {
-                    s0[i][0] = e0 - t10[i];
-                    s1[i][0] = e1 - t11[i];
-                    e2[i][0] = s0[i][0] + (t02[i] - cf.p012);
-                }
-            }
-            auto do_class = [&](auto czc, Acc& acc) {
-                constexpr int cz = decltype(czc)::value;
-                float g[3][3], r[3][3];
-#pragma unroll
-                for (int i = 0; i < 3; ++i) {
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) {
-                        const int cx = i - 1, cy = j - 1;
-                        g[i][j] = 0.0f;
-                        r[i][j] = 0.0f;
-                        if (!(ROWS & (1 << j)) || !Stencil<Q>::has(cx, cy, cz)) continue;
-                        float small =
-                            cz == 0 ? s0[i][j] : (cz > 0 ? e2[i][j] + s1[i][j] : e2[i][j] - s1[i][j]);
-                        if (cx == 0 && cy == 0 && cz == 0) small += rc0;
-                        const float vv = rho_src + small;
-                        const int sh = cx * cx + cy * cy + cz * cz;
-                        g[i][j] = kSepW ? vv : (sh == 0 ? 12.0f * vv : (sh == 1 ? vv + vv : vv));
-                    }
-                }
-                {
-                    if (any_iface) {
-#pragma unroll
-                        for (int i = 0; i < 3; ++i)
-#pragma unroll
-                            for (int j = 0; j < 3; ++j) {
-                                const int cx = i - 1, cy = j - 1, sh = cx * cx + cy * cy + cz * cz;
-                                if (!(ROWS & (1 << j))) continue;
-                                const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
-                                const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
-                                r[i][j] = sh == 0 ? aR * g[i][j] : fmaf(aR, g[i][j], dks * fc);
-                            }
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < 3; ++i)
-#pragma unroll
-                            for (int j = 0; j < 3; ++j)
-                                if (ROWS & (1 << j)) r[i][j] = aR * g[i][j];
-                    }
-                }
-                if constexpr (ROWS == 7) {
-                    if (any_reflect && reflect) {
-#pragma unroll
-                        for (int i = 0; i < 3; ++i)
-#pragma unroll
-                            for (int j = 0; j < 3; ++j) {
-                                const int cx = i - 1, cy = j - 1;
-                                if (!Stencil<Q>::has(cx, cy, cz)) continue;
-                                const bool into = (wx0 && cx < 0) || (wx1 && cx > 0) || (wy0 && cy < 0) ||
-                                                  (wy1 && cy > 0) || (wz0 && cz < 0) || (wz1 && cz > 0);
-                                if (!into) continue;
-                                const float f = kSepW ? static_cast<float>((cx == 0 ? 4 : 1) * (cy == 0 ? 4 : 1) *
-                                                                           (cz == 0 ? 4 : 1))
-                                                      : 1.0f;
-                                add_pop(accC, f * g[i][j], f * r[i][j], -cx, -cy, -cz);
-                            }
-                    }
-                }
-                // x streaming: destination x receives cx=+1 from lane-1 and cx=-1 from lane+1
-                float X0[3], X1[3], X2[3], XR[3];
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const int cy = j - 1;
-                    X0[j] = X1[j] = X2[j] = XR[j] = 0.0f;
-                    if (!(ROWS & (1 << j))) continue;
-                    if (Stencil<Q>::has(1, cy, cz)) {
-                        const float gl = __shfl_up_sync(kFull, g[2][j], 1);
-                        const float gr = __shfl_down_sync(kFull, g[0][j], 1);
-                        X2[j] = gl + gr;
-                        X0[j] = kSepW ? fmaf(4.0f, g[1][j], X2[j]) : X2[j] + g[1][j];
-                        X1[j] = gl - gr;
-                        const float rl = __shfl_up_sync(kFull, r[2][j], 1);
-                        const float rr_ = __shfl_down_sync(kFull, r[0][j], 1);
-                        XR[j] = kSepW ? fmaf(4.0f, r[1][j], rl + rr_) : (rl + rr_) + r[1][j];
-                    } else {
-                        X0[j] = g[1][j];
-                        XR[j] = r[1][j];
-                    }
-                }
-                if constexpr ((ROWS & 2) != 0) {
-                    // cy = 0 row stays in this column: add to the destination's sums now
-                    constexpr float f = kSepW ? (cz == 0 ? 16.0f : 4.0f) : 1.0f;
-                    acc.rho = fmaf(f, X0[1], acc.rho);
-                    acc.jx = fmaf(f, X1[1], acc.jx);
-                    acc.xx = fmaf(f, X2[1], acc.xx);
-                    acc.red = fmaf(f, XR[1], acc.red);
-                    if (cz != 0) {
-                        acc.jz = fmaf(cz * f, X0[1], acc.jz);
-                        acc.xz = fmaf(cz * f, X1[1], acc.xz);
-                        acc.zz = fmaf(f, X0[1], acc.zz);
-                    }
-                }
-                // cy = +1 goes to row w+1 (slot 0), cy = -1 to row w-1 (slot 1)
-                constexpr int cls = cz + 1;
-                if constexpr ((ROWS & 4) != 0) {
-                    float* b0 = xb_self + ((cls * 2 + 0) * 4) * (W * 32);
-                    b0[0 * W * 32] = X0[2];
-                    b0[1 * W * 32] = X1[2];
-                    b0[2 * W * 32] = X2[2];
-                    b0[3 * W * 32] = XR[2];
-                }
-                if constexpr ((ROWS & 1) != 0) {
-                    float* b1 = xb_self + ((cls * 2 + 1) * 4) * (W * 32);
-                    b1[0 * W * 32] = X0[0];
-                    b1[1 * W * 32] = X1[0];
-                    b1[2 * W * 32] = X2[0];
-                    b1[3 * W * 32] = XR[0];
-                }
-            };
-            do_class(std::integral_constant<int, -1>{}, accP);
-            do_class(std::integral_constant<int, 0>{}, accC);
-            do_class(std::integral_constant<int, 1>{}, accN);
-        };
-        if (w == 0) emit(std::integral_constant<int, 4>{});
-        else if (w == W - 1) emit(std::integral_constant<int, 1>{});
-        else emit(std::integral_constant<int, 7>{});
-        __syncthreads();
-
-        // (4) y streaming into destination rows
-        auto gather = [&](auto czc, Acc& acc) {
-            constexpr int cz = decltype(czc)::value;
-            constexpr int cls = cz + 1;
-            constexpr float f = (kSepW && cz == 0) ? 4.0f : 1.0f;
-            const float* p0 = xb_self - 32 + ((cls * 2 + 0) * 4) * (W * 32);
-            const float* m1 = xb_self + 32 + ((cls * 2 + 1) * 4) * (W * 32);
-            const float P0 = p0[0], P1 = p0[W * 32], P2 = p0[2 * W * 32], PR = p0[3 * W * 32];
-            const float M0 = m1[0], M1 = m1[W * 32], M2 = m1[2 * W * 32], MR = m1[3 * W * 32];
-            const float s00 = P0 + M0;
-            const float s10 = P1 + M1;
-            const float d00 = P0 - M0;
-            acc.rho = fmaf(f, s00, acc.rho);
-            acc.jx = fmaf(f, s10, acc.jx);
-            acc.xx = fmaf(f, P2 + M2, acc.xx);
-            acc.jy = fmaf(f, d00, acc.jy);
-            acc.xy = fmaf(f, P1 - M1, acc.xy);
-            acc.yy = fmaf(f, s00, acc.yy);
-            acc.red = fmaf(f, PR + MR, acc.red);
-            if (cz != 0) {
-                acc.jz += cz * s00;
-                acc.xz += cz * s10;
-                acc.yz += cz * d00;
-                acc.zz += s00;
-            }
-        };
-        const bool dest_row = (w >= 1 && w <= W - 2);
-        if (dest_row) gather(std::integral_constant<int, -1>{}, accP);
-
-        // (5) destination plane k-1 is complete: moments (lbm.cuh:239-261), store, boundary
-        const int d = k - 1;
-        if (dest_thread && d >= zd0 && d < zd1) {
-            {
-                constexpr float S = kSepW ? 216.0f : 36.0f;
-                constexpr float sc = 1.0f / S;
-                // correctly rounded mass quotients (no systematic bias), plain scaling for the rest
-                const float q0 = accP.rho * sc, q1 = accP.red * sc;
-                accP.rho = fmaf(fmaf(-q0, S, accP.rho), sc, q0);
-                accP.red = fmaf(fmaf(-q1, S, accP.red), sc, q1);
-                accP.jx *= sc; accP.jy *= sc; accP.jz *= sc;
-                accP.xx *= sc; accP.xy *= sc; accP.yy *= sc; accP.yz *= sc; accP.zz *= sc; accP.xz *= sc;
-            }
-            const float rho = accP.rho;
-            const float rr = accP.red;
-            const float rb = rho - rr;
-            const float inv = fast_rcp(rho);
-            float Fbx = 0.0f, Fby = 0.0f, Fbz = 0.0f;
-            if (P.forced) {
-                Fbx = rho * P.g[0];
-                Fby = rho * P.g[1];
-                Fbz = rho * P.g[2];
-            }
-            const float ux = (accP.jx + 0.5f * Fbx) * inv;
-            const float uy = (accP.jy + 0.5f * Fby) * inv;
-            const float uz = (accP.jz + 0.5f * Fbz) * inv;
-            const float ctr = cs2 * rho;
-            float pi[6];
-            pi[0] = (accP.xx - ctr) - rho * ux * ux;
-            pi[1] = accP.xy - rho * ux * uy;
-            pi[2] = (accP.yy - ctr) - rho * uy * uy;
-            pi[3] = accP.yz - rho * uy * uz;
-            pi[4] = (accP.zz - ctr) - rho * uz * uz;
-            pi[5] = accP.xz - rho * ux * uz;
-            if (P.forced) {
-                pi[0] += ux * Fbx;
-                pi[1] += 0.5f * (ux * Fby + uy * Fbx);
-                pi[2] += uy * Fby;
-                pi[3] += 0.5f * (uy * Fbz + uz * Fby);
-                pi[4] += uz * Fbz;
-                pi[5] += 0.5f * (ux * Fbz + uz * Fbx);
-            }
-            if (P.ratio) {
-                const float Kc = (rr * P.kappa_r + rb * P.kappa_b) * cs2;
-                pi[0] -= Kc;
-                pi[2] -= Kc;
-                pi[4] -= Kc;
-            }
-            finalize_store<S>(P, xs, ys, d, rr, rb, ux, uy, uz, pi);
-
-            if (P.do_bc && ia >= 0) {
-                // inlet / outlet functors fused into the first and last fluid layer
-                const int pa = ia == 0 ? xs : (ia == 1 ? ys : d);
-                const int na = ia == 0 ? nx : (ia == 1 ? ny : nz);
-                if (pa == 1 || pa == na - 2) {
-                    const bool inlet = pa == 1;
-                    const int gx = ia == 0 ? (inlet ? 0 : nx - 1) : xs;
-                    const int gy = ia == 1 ? (inlet ? 0 : ny - 1) : ys;
-                    const int gz = ia == 2 ? (inlet ? 0 : nz - 1) : d;
-                    const long long og = static_cast<long long>(gz) * P.plane + static_cast<long long>(gy) * P.pitch + gx;
-                    float orr, orb, oux, ouy, ouz;
-                    if (inlet) {
-                        // jet/boundary_conditions.cuh:16-39 (+ seeded per-node noise)
-                        const int t0 = ia == 0 ? ys : xs;
-                        const int t1 = ia == 2 ? ys : d;
-                        const float du = static_cast<float>(t0) - P.jet_c0;
-                        const float dv = static_cast<float>(t1) - P.jet_c1;
-                        const float m = (du * du + dv * dv) <= (P.jet_radius * P.jet_radius) ? 1.0f : 0.0f;
-                        orr = P.jet_blue ? (1.0f - m) * P.rho_r0 : m * P.rho_r0;
-                        orb = P.jet_blue ? m * P.rho_b0 : (1.0f - m) * P.rho_b0;
-                        float gu[3] = {0.0f, 0.0f, 0.0f};
-                        if (m != 0.0f) {
-                            if (P.noise_amp != 0.0f) {
-                                const unsigned long long node = static_cast<unsigned long long>(gx) +
-                                                                static_cast<unsigned long long>(gy) * nx +
-                                                                static_cast<unsigned long long>(gz) * nx * ny;
-                                gu[0] = m * P.noise_amp * noise_xi(P.seed, P.step, node, 0);
-                                gu[1] = m * P.noise_amp * noise_xi(P.seed, P.step, node, 1);
-                                gu[2] = m * P.noise_amp * noise_xi(P.seed, P.step, node, 2);
-                            }
-                        }
-                        oux = gu[0] + (ia == 0 ? m * P.jet_velocity : 0.0f);
-                        ouy = gu[1] + (ia == 1 ? m * P.jet_velocity : 0.0f);
-                        ouz = gu[2] + (ia == 2 ? m * P.jet_velocity : 0.0f);
-                    } else if (P.outlet == MBCG_OUTLET_ZERO_GRADIENT) {
-                        orr = rr; orb = rb; oux = ux; ouy = uy; ouz = uz;
-                    } else {
-                        // convective outlet (jet/boundary_conditions.cuh:45-109), old ghost from A
-                        float ov[NF];
-                        if (ia == 2 && col_in_box) {
-                            ov[0] = Codec<S>::to_f(rb_box(st, 0)[bR]);
-                            ov[1] = Codec<S>::to_f(rb_box(st, 1)[bR]);
-#pragma unroll
-                            for (int f = 2; f < NF; ++f) ov[f] = Codec<S>::to_f(m_box(st, f)[bM]);
-                        } else {
-                            load_global<S>(P, og, ov);
-                        }
-                        Node<S> on{};
-                        decode<S>(P, ov, on);
-                        const float ua = ia == 0 ? ux : (ia == 1 ? uy : uz);
-                        const float uc = fminf(fmaxf(ua, 0.0f), 1.0f);
-                        if (on.rr + on.rb <= 1.0e-20f) {
-                            orr = rr; orb = rb; oux = ux; ouy = uy; ouz = uz;
-                        } else {
-                            orr = on.rr - uc * (on.rr - rr);
-                            orb = on.rb - uc * (on.rb - rb);
-                            oux = on.ux - uc * (on.ux - ux);
-                            ouy = on.uy - uc * (on.uy - uy);
-                            ouz = on.uz - uc * (on.uz - uz);
-                        }
-                    }
-                    finalize_store<S>(P, gx, gy, gz, orr, orb, oux, ouy, ouz, pi);
-                }
-            }
-        }
-        if (dest_row) {
-            gather(std::integral_constant<int, 0>{}, accC);
-            gather(std::integral_constant<int, 1>{}, accN);
-        }
-        accP = accC;
-        accC = accN;
-        accN.zero();
-    }
-}
-
-} // namespace
-
-// ------------------------------------------------------------------ host launcher
-template <int Q, typename S, int W, bool kTMA>
-static cudaError_t launch_one(const StepParams& P, const TensorMaps& T, cudaStream_t s) {
-    using G = Geo<S, W>;
-    auto kern = step_kernel<Q, S, W, kTMA>;
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, G::smem);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
-    dim3 block(32, W, 1);
-    dim3 grid((P.nx - 2 + kTX - 1) / kTX, (P.ny - 2 + W - 3) / (W - 2), (P.nz - 2 + P.zchunk - 1) / P.zchunk);
-    kern<<<grid, block, G::smem, s>>>(P, T);
-    return cudaGetLastError();
-}
-
-template <typename S>
-static cudaError_t launch_prec(int q, bool tma, const StepParams& P, const TensorMaps& T, cudaStream_t s) {
-    if (q == 27) return tma ? launch_one<27, S, kStepW, true>(P, T, s) : launch_one<27, S, kStepW, false>(P, T, s);
-    return tma ? launch_one<19, S, kStepW, true>(P, T, s) : launch_one<19, S, kStepW, false>(P, T, s);
-}
-
-cudaError_t launch_step(int q, int precision, bool tma, const StepParams& P, const TensorMaps& T, cudaStream_t s) {
     switch (precision) {
-    case MBCG_FP16: return launch_prec<__half>(q, tma, P, T, s);
-    case MBCG_BF16: return launch_prec<__nv_bfloat16>(q, tma, P, T, s);
-    default: return launch_prec<float>(q, tma, P, T, s);
+    case MBCG_FP16: return launch_step_q19_f16(tma, w, P, T, s);
+    case MBCG_BF16: return launch_step_q19_bf16(tma, w, P, T, s);
+    default: return launch_step_q19_f32(tma, w, P, T, s);
     }
 }
 
-int step_smem_bytes(int precision) {
-    return precision == MBCG_FP32 ? Geo<float, kStepW>::smem : Geo<__half, kStepW>::smem;
+int step_smem_bytes(int precision, int w) {
+    if (precision == MBCG_FP32) return w == kStepWSmall ? Geo<float, kStepWSmall>::smem : Geo<float, kStepW>::smem;
+    return w == kStepWSmall ? Geo<__half, kStepWSmall>::smem : Geo<__half, kStepW>::smem;
 }
-
-int step_box_rows() { return kStepW; }
-int step_tile_x() { return kTX; }
-int step_rb_box_x() { return kRBX; }
-int step_m_box_x() { return kMX; }
 
 } // namespace mbcg

@@ -260,6 +260,9 @@ _PROTOS = {
     "mbcg_copy_in": (ctypes.c_int, [_VP, _VP * NFIELDS, _VP]),
     "mbcg_diagnostics": (ctypes.c_int, [_VP, _P(Diag), _VP]),
     "mbcg_status": (ctypes.c_int, [_VP, _P(ctypes.c_int32)]),
+    "mbcg_get_shape": (ctypes.c_int, [_VP, _P(ctypes.c_int32), _P(ctypes.c_int32)]),
+    "mbcg_set_shape": (ctypes.c_int, [_VP, ctypes.c_int32, ctypes.c_int32]),
+    "mbcg_autotune": (ctypes.c_int, [_VP, ctypes.c_int32, _P(ctypes.c_double), _VP]),
     "mbcg_rcs_moments": (ctypes.c_int, [_P(Params), _P(Moments), _P(Moments), ctypes.c_int64, _VP]),
     "mbcg_bc_moments": (ctypes.c_int, [_P(Params), _P(Moments), _P(Moments), ctypes.c_int64, _VP]),
     "mbcg_init_moments": (ctypes.c_int, [_P(Params), _P(Moments), _VP]),
@@ -387,6 +390,23 @@ class Case:
 
     def launches_per_step(self) -> int:
         return int(self.lib.mbcg_launches_per_step(self.handle))
+
+    @property
+    def shape(self) -> tuple:
+        """(block_rows, zchunk) of the step launches."""
+        w, z = ctypes.c_int32(0), ctypes.c_int32(0)
+        self.lib.check(self.lib.mbcg_get_shape(self.handle, ctypes.byref(w), ctypes.byref(z)), "mbcg_get_shape")
+        return int(w.value), int(z.value)
+
+    def set_shape(self, block_rows: int, zchunk: int):
+        self.lib.check(self.lib.mbcg_set_shape(self.handle, int(block_rows), int(zchunk)), "mbcg_set_shape")
+
+    def autotune(self, repeats: int = 3, stream=None) -> float:
+        """Measure the candidate launch shapes on this case and keep the fastest; returns ms/step."""
+        ms = ctypes.c_double(0.0)
+        self.lib.check(self.lib.mbcg_autotune(self.handle, int(repeats), ctypes.byref(ms), _stream_ptr(stream)),
+                       "mbcg_autotune")
+        return float(ms.value)
 
 
 def moments_from_tensors(tensors: Sequence, pitch: int, precision: int = FP32) -> Moments:
