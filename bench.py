@@ -15,6 +15,14 @@ L2, so no explicit L2 flush is needed between timed steps.
 --impl reference times the reference algorithm on the host cores instead: the CPU oracle's
 FP32 restatement of the reference step (bit-exact with the reference's own code on the
 golden fixtures), all host threads, on a z-slab sample of the same jet.
+
+Serving (the "serving" object of the JSON line): a seeded stream of bubble and Rayleigh-Taylor
+requests with Poisson arrivals runs once through the continuous-batching server and once one
+request at a time through the single-case API (create, initial condition, steps, diagnostics,
+destroy); both report cases/s, p50/p99 time to completion and aggregate MLUPS.  The full
+workload (--serving full) is 256 requests at 20/s with 500-5000 steps each; the default sample
+keeps the size and case distributions but scales every step count by 1/10 and the arrival rate
+by 10, so the offered load (node updates per second of arrivals) is the same.
 """
 from __future__ import annotations
 
@@ -191,6 +199,105 @@ def cpu_leg(budget_s: float, threads: int, real_bytes: int = 4) -> dict:
                                       f"{'FP32' if real_bytes == 4 else 'FP64'} oracle, {dt:.1f} s"}
 
 
+# ---------------------------------------------------------------- serving workload
+def serving_requests(n: int, rate: float, step_scale: float, seed: int = 20240):
+    """Seeded request stream: Poisson arrivals at `rate`/s; bubble (config-0 physics, radius L/4,
+    L log-uniform in [32, 192]) or Rayleigh-Taylor (config-1 physics, L x L x 4L, L log-uniform
+    in [32, 128]) with equal probability; D3Q19 or D3Q27 and FP32 or FP16 moments by coin flip;
+    steps uniform in [500, 5000] times step_scale."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for _ in range(n):
+        t += rng.exponential(1.0 / rate)
+        bubble = rng.random() < 0.5
+        q = 19 if rng.random() < 0.5 else 27
+        prec = mbcg.FP32 if rng.random() < 0.5 else mbcg.FP16
+        steps = max(1, int(round(rng.uniform(500, 5000) * step_scale)))
+        if bubble:
+            L = int(round(np.exp(rng.uniform(np.log(32), np.log(192)))))
+            p = mbcg.bubble_params(L, q=q, radius=0.25 * L, precision=prec)
+        else:
+            L = int(round(np.exp(rng.uniform(np.log(32), np.log(128)))))
+            p = mbcg.rti_params(L, q=q, precision=prec)
+        out.append({"t": t, "p": p, "steps": steps, "kind": "bubble" if bubble else "rti", "L": L})
+    return out
+
+
+def _pct(v, q):
+    return float(np.percentile(np.asarray(v), q)) if v else None
+
+
+def serve_batched(reqs, policy=mbcg.POLICY_FIFO) -> dict:
+    with mbcg.Server(policy=policy) as srv:
+        t0 = time.perf_counter()
+        ids = []
+        for r in reqs:
+            delay = r["t"] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            ids.append(srv.submit(r["p"], r["steps"]))
+        srv.drain()
+        infos = [srv.poll(i) for i in ids]
+        st = srv.stats().as_dict()
+    ttc = [i.t_done - i.t_submit for i in infos]
+    span = max(i.t_done for i in infos) - min(i.t_submit for i in infos)
+    work = sum(r["p"].active_nodes() * r["steps"] for r in reqs)
+    return {"cases_per_s": len(reqs) / span, "p50_s": _pct(ttc, 50), "p99_s": _pct(ttc, 99), "makespan_s": span,
+            "mlups": work / span / 1e6, "failed": sum(i.state != mbcg.REQ_DONE for i in infos),
+            "compositions": st["compositions"], "replays": st["replays"], "zchunk_last": st["zchunk"],
+            "cost_model_ns_per_plane": st["plane_ns"], "tile_overhead_planes": st["tile_overhead_planes"],
+            "arena_peak_gb": st["arena_peak_bytes"] / 1e9,
+            "mass": [(i.diag.mass_r, i.diag.mass_b) for i in infos],
+            "nonfinite": sum(i.diag.nonfinite for i in infos)}
+
+
+def serve_sequential(reqs, torch) -> dict:
+    t0 = time.perf_counter()
+    ttc, done, mass = [], [], []
+    for r in reqs:
+        now = time.perf_counter() - t0
+        if now < r["t"]:
+            time.sleep(r["t"] - now)
+        with mbcg.Case(r["p"]) as c:
+            c.init()
+            c.step(r["steps"])
+            d = c.diagnostics()
+        fin = time.perf_counter() - t0
+        done.append(fin)
+        ttc.append(fin - r["t"])
+        mass.append((d["mass_r"], d["mass_b"]))
+    span = max(done) - reqs[0]["t"]
+    work = sum(r["p"].active_nodes() * r["steps"] for r in reqs)
+    return {"cases_per_s": len(reqs) / span, "p50_s": _pct(ttc, 50), "p99_s": _pct(ttc, 99), "makespan_s": span,
+            "mlups": work / span / 1e6, "mass": mass}
+
+
+def serving_leg(mode: str, torch) -> dict:
+    if mode == "full":
+        n, rate, scale = 256, 20.0, 1.0
+    else:
+        n, rate, scale = 64, 200.0, 0.1
+    reqs = serving_requests(n, rate, scale)
+    b = serve_batched(reqs)
+    bs = serve_batched(reqs, mbcg.POLICY_SJF)
+    bs.pop("mass")
+    s = serve_sequential(reqs, torch)
+    rel = 0.0
+    for (br, bb), (sr, sb) in zip(b.pop("mass"), s.pop("mass")):
+        rel = max(rel, abs(br - sr) / abs(sr), abs(bb - sb) / abs(sb))
+    return {"workload": ("full: " if mode == "full" else "sample: ") +
+            f"{n} requests, Poisson {rate:g}/s, bubble L in [32,192] or RTI LxLx4L L in [32,128] (log-uniform), "
+            f"Q19/Q27 and FP32/FP16 by coin flip, steps U[500,5000] x {scale:g}",
+            "batched": b, "sequential": s, "cases_per_s_ratio": b["cases_per_s"] / s["cases_per_s"],
+            "policy": "FIFO admission with backfill (all requests that fit are live)",
+            "batched_sjf": {k: bs[k] for k in ("cases_per_s", "p50_s", "p99_s", "mlups", "makespan_s")},
+            "batched_sjf_policy": "shortest job first with aging, live set capped at 4 waves of tiles",
+            "accuracy": {"max_rel_phase_mass_diff_batched_vs_sequential": rel,
+                         "note": "same physics in both; the batch kernel and the single-case kernel are "
+                                 "separate compilations (parity gate rel L2 1e-5, tests/test_gpu_server.py)"}}
+
+
 def reference_arm(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -228,6 +335,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--forms", default="fp16,bf16")
     ap.add_argument("--nz", type=int, default=1024, help="fluid planes of the jet (profiling uses fewer)")
+    ap.add_argument("--serving", default="sample", choices=["off", "sample", "full"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -279,6 +387,7 @@ def main() -> None:
                        "roofline_frac": BYTES_PER_NODE[prec] * nodes / (t / args.steps) / 1e9 / peak}
 
     e2e = time_e2e(p, args.e2e_steps, torch) if rank == 0 and args.e2e_steps > 0 else None
+    serving = serving_leg(args.serving, torch) if rank == 0 and args.serving != "off" else None
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_leg(args.cpu_budget, os.cpu_count() or 1)
@@ -296,6 +405,7 @@ def main() -> None:
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_node": BYTES_PER_NODE[mbcg.FP32]},
             "forms": forms,
+            "serving": serving,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps * launches,

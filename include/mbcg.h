@@ -60,7 +60,7 @@ typedef struct CUstream_st *mbcg_stream_t; /* == cudaStream_t; NULL = legacy def
 #define MBCG_E_INVALID    -1 /* bad parameter                        */
 #define MBCG_E_CUDA       -2 /* a CUDA runtime / driver call failed    */
 #define MBCG_E_NOMEM      -3 /* device allocation failed               */
-#define MBCG_E_TIMEOUT    -4 /* a bounded device wait gave up           */
+#define MBCG_E_TIMEOUT    -4 /* a bounded device wait or a server wait gave up */
 #define MBCG_E_UNSUPPORTED -5
 
 /* ---- case parameters (runtime replacement of the reference's constants.cuh) --------- */
@@ -205,6 +205,90 @@ int mbcg_init_moments(const mbcg_params *p, const mbcg_moments *a, mbcg_stream_t
  * capture.  All calls share the array: calls that overlap on the GPU race, so serialise them
  * (same stream, or synchronise between them).  Synchronous: returns once *out is filled. */
 int mbcg_diagnostics_static(const mbcg_params *p, const mbcg_moments *a, mbcg_diag *out, mbcg_stream_t s);
+
+/* ---- serving: continuous batching of many lattices on one GPU ------------------------
+ * No counterpart in the reference (one lattice per process, main.cu:25-55).  A server owns a
+ * device arena and a worker thread.  Requests (a case and a step count) queue on submit and are
+ * admitted while a slot and arena space are free, in the order the policy gives (with backfill
+ * a later request that fits may pass one that does not yet).  All resident lattices advance
+ * together: one persistent batch-kernel launch per time step runs every live lattice's tiles
+ * from one flat queue, and each batch composition (the set of live lattices) is captured once
+ * as a CUDA graph of chunk_steps launches that is replayed until the composition changes.  A
+ * lattice computes the same arithmetic alone or in any mix (its tiles never read another
+ * lattice's data), so its result is identical, bit for bit, whatever else runs beside it. */
+typedef struct mbcg_server mbcg_server;
+
+typedef struct mbcg_server_config {
+    int64_t arena_bytes;    /* device memory for resident states (0: 70% of the free memory)  */
+    int32_t max_live;       /* lattices resident at once (0: 64; at most 4096)                 */
+    int32_t chunk_steps;    /* launches per graph replay, the admission granularity (0: 16)    */
+    int32_t keep_results;   /* 1: finished states stay resident until fetched or released      */
+    int32_t backfill;       /* 1: admit later requests that fit while an earlier one waits     */
+    int32_t zchunk;         /* z depth of the tiles (0: the planner picks one per composition:
+                               the depth whose greedy schedule of all live tiles on the SMs,
+                               under the cost model, gives the shortest launch)                */
+    int32_t calibrate;      /* 1: measure the cost model (time of one tile plane per kernel body
+                               and lattice, fixed cost per tile) at start-up; 0: defaults      */
+    int32_t policy;         /* MBCG_POLICY_*: admission order (default FIFO: highest throughput;
+                               SJF: lower median time to completion)                          */
+    int32_t fill_waves;     /* shortest job first admits while the live tiles (at 16 planes)
+                               fill fewer than fill_waves waves of one CTA per SM (0: 4)      */
+} mbcg_server_config;
+
+#define MBCG_POLICY_FIFO 0  /* arrival order                                                   */
+#define MBCG_POLICY_SJF  1  /* shortest estimated remaining time first, with aging: a request's
+                               wait counts against its work at the server's throughput        */
+
+#define MBCG_REQ_QUEUED  0
+#define MBCG_REQ_RUNNING 1
+#define MBCG_REQ_DONE    2
+#define MBCG_REQ_FAILED  3
+
+typedef struct mbcg_request_info {
+    int64_t id;
+    int32_t state;          /* MBCG_REQ_*                                                      */
+    int32_t status;         /* the lattice's device status word at completion (0 = ok)         */
+    int64_t steps;          /* steps requested                                                 */
+    int64_t steps_done;
+    double t_submit;        /* seconds since the server started: submitted,                   */
+    double t_admit;         /* admitted (its initial condition enqueued),                      */
+    double t_done;          /* final state and diagnostics complete on the GPU (-1 if not)     */
+    uint64_t state_hash;    /* order-independent 64-bit hash of the final fluid-node state     */
+    mbcg_diag diag;         /* FP64 diagnostics of the final state                             */
+} mbcg_request_info;
+
+typedef struct mbcg_server_stats {
+    int64_t submitted, completed, failed, live, queued;
+    int64_t node_updates;   /* fluid-node updates completed                                    */
+    int64_t compositions;   /* distinct batch compositions (graph captures)                    */
+    int64_t replays;        /* graph replays                                                   */
+    int64_t arena_bytes, arena_peak_bytes;
+    int32_t zchunk;         /* tile z depth the planner chose for the current composition      */
+    int32_t reserved;
+    double plane_ns[10];    /* cost model: ns per tile plane of each batch-kernel body, in the
+                               order Q19 FP32/FP16/BF16, Q27 FP32/FP16/BF16 (every feature),
+                               Q19 FP32/FP16, Q27 FP32/FP16 (fully periodic, unforced)          */
+    double tile_overhead_planes; /* cost model: fixed cost of a tile, in planes                */
+    double busy_s;          /* first admission to the last completion                          */
+} mbcg_server_stats;
+
+void mbcg_server_config_default(mbcg_server_config *cfg);
+int mbcg_server_create(const mbcg_server_config *cfg, mbcg_server **out);
+/* Stops admitting, finishes the work in flight, frees everything. */
+int mbcg_server_destroy(mbcg_server *s);
+/* Queues a request (thread-safe, does not block).  The case's ic selects its initial condition;
+ * a lattice larger than the whole arena is rejected with MBCG_E_NOMEM. */
+int mbcg_server_submit(mbcg_server *s, const mbcg_params *p, int64_t nsteps, int64_t *id);
+int mbcg_server_poll(mbcg_server *s, int64_t id, mbcg_request_info *out);
+/* Blocks until request id is done or failed, or timeout_s passes (MBCG_E_TIMEOUT). */
+int mbcg_server_wait(mbcg_server *s, int64_t id, double timeout_s, mbcg_request_info *out);
+/* Blocks until nothing is queued or running. */
+int mbcg_server_drain(mbcg_server *s, double timeout_s);
+/* keep_results: copies a finished state to 11 dense FP32 host arrays (as mbcg_copy_out) and
+ * keeps it resident; mbcg_server_release frees it. */
+int mbcg_server_fetch(mbcg_server *s, int64_t id, float *const host[MBCG_NFIELDS]);
+int mbcg_server_release(mbcg_server *s, int64_t id);
+int mbcg_server_get_stats(mbcg_server *s, mbcg_server_stats *out);
 
 /* Active (fluid) node count used by the MLUPS definition, (nx-2)(ny-2)(nz-2)
  * (utilities/mlups_count.cuh:24-29). */

@@ -225,6 +225,14 @@ bool tuned_shape(const mbcg_params& p, int* w, int* zchunk) {
 } // namespace
 
 void mbcg::set_last_error(const std::string& msg) { g_err = msg; }
+int mbcg::validate_params(const mbcg_params* p) { return validate(p); }
+void mbcg::fill_step_physics(const mbcg_params& p, StepParams& P) { fill_physics(p, P); }
+bool mbcg::state_tma_capable(const mbcg_params& p, const void* const* f, long long pitch) {
+    return tma_capable(p, f, pitch, p.precision);
+}
+int mbcg::encode_state_maps(const mbcg_params& p, const void* const* f, long long pitch, int W, TensorMaps& T) {
+    return encode_maps(p, f, pitch, p.precision, W, T);
+}
 
 struct mbcg_case {
     mbcg_params p;

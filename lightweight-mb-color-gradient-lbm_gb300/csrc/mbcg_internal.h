@@ -49,6 +49,12 @@ cudaError_t launch_from_dense(int precision, const StepParams& P, int field, con
 
 // sets the message mbcg_last_error() returns on the calling thread (mbcg_capi.cu)
 void set_last_error(const std::string& msg);
+// parameter checks, the step's constant chain and TMA descriptors, shared by the case API and
+// the server (mbcg_capi.cu); validate_params sets the last-error message on failure
+int validate_params(const mbcg_params* p);
+void fill_step_physics(const mbcg_params& p, StepParams& P);
+bool state_tma_capable(const mbcg_params& p, const void* const* f, long long pitch);
+int encode_state_maps(const mbcg_params& p, const void* const* f, long long pitch, int W, TensorMaps& T);
 
 constexpr int kDiagSlots = 12; // mass_r, mass_b, mom x/y/z, p_in sum, n_in, p_out sum, n_out, nonfinite, nodes, spare
 

@@ -1,0 +1,1114 @@
+// mbcg_server.cu -- continuous-batching server: many lattices resident in one device arena,
+// advanced together by the persistent batch kernel (mbcg_batch.cu), one CUDA graph per batch
+// composition.  The C ABI is declared in include/mbcg.h (mbcg_server_*).
+//
+// Threads.  Client threads submit, poll, wait, fetch and release under the server mutex.  One
+// worker thread owns the compute stream: it admits queued requests (slot + arena space, first
+// fit in arrival order, optional backfill), initialises them, captures a graph whenever the set
+// of live lattices changes, replays it chunk after chunk (at most two chunks in flight), and
+// retires finished lattices (status, diagnostics, state hash).  All host bookkeeping of a
+// lattice's progress is exact (each replay advances it by a known number of steps), so the
+// worker never waits for the GPU except to bound the work in flight.
+//
+// Memory.  Every upload the GPU reads (tile queue, per-slot progress, lattice tables) goes
+// through pinned staging buffers that are not rewritten until the copy that reads them has
+// executed (an event per staging buffer), and every device copy is stream-ordered on the
+// compute stream, so a replay never sees a half-updated table.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "mbcg_batch.h"
+#include "mbcg_internal.h"
+
+using namespace mbcg;
+
+namespace {
+
+constexpr int kRing = 4;         // pinned staging buffers per kind of upload
+constexpr int kMaxLiveCap = 4096; // slot index fits the 16-bit tile field
+constexpr size_t kAlign = 256;
+
+int fail(int code, const std::string& msg) {
+    set_last_error(msg);
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MBCG_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// First-fit allocator over one device allocation.
+class Arena {
+  public:
+    void reset(size_t size) {
+        size_ = size;
+        free_.clear();
+        if (size) free_[0] = size;
+        used_ = peak_ = 0;
+    }
+    bool alloc(size_t n, size_t* off) {
+        n = align_up(n, kAlign);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *off = it->first;
+                const size_t rest = it->second - n;
+                const size_t start = it->first + n;
+                free_.erase(it);
+                if (rest) free_[start] = rest;
+                used_ += n;
+                peak_ = std::max(peak_, used_);
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t n) {
+        n = align_up(n, kAlign);
+        used_ -= n;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t size() const { return size_; }
+    size_t peak() const { return peak_; }
+
+  private:
+    size_t size_ = 0, used_ = 0, peak_ = 0;
+    std::map<size_t, size_t> free_;
+};
+
+// Pinned staging buffer reused round-robin; `ev` marks the copy that last read it.
+struct Staging {
+    void* host = nullptr;
+    size_t cap = 0;
+    cudaEvent_t ev = nullptr;
+    bool pending = false;
+};
+
+struct Request {
+    int64_t id = 0;
+    mbcg_params p{};
+    int64_t steps = 0;
+    int state = MBCG_REQ_QUEUED;
+    int status = 0;
+    double t_submit = 0, t_admit = -1, t_done = -1;
+    int64_t steps_done = 0;
+    uint64_t hash = 0;
+    mbcg_diag diag{};
+    // while resident
+    int slot = -1;
+    size_t off = 0, bytes = 0;
+    long long pitch = 0, plane = 0, fstride = 0;
+    int es = 4;
+    int features = 0;
+    int zchunk = 32;
+    void* fields[2][NF] = {};
+    int cur = 0;             // parity of the state holding step steps_done
+    int64_t nodes = 0;
+    double* d_partials = nullptr;
+    double* d_result = nullptr; // kDiagSlots doubles, then the hash (as 8 bytes), then the status word
+    int nparts = 0;
+    cudaEvent_t done_ev = nullptr;
+    bool retiring = false;   // finished on the host clock; waiting for done_ev
+    bool resident = false;   // arena memory held
+    int fetching = 0;        // fetches in progress (release waits for them)
+    double* h_result = nullptr; // pinned copy of d_result
+    int64_t nodes_estimate() const { return static_cast<int64_t>(p.nx - 2) * (p.ny - 2) * (p.nz - 2); }
+};
+
+} // namespace
+
+struct mbcg_server {
+    mbcg_server_config cfg{};
+    int device = 0, nsm = 152;
+    cudaStream_t st = nullptr, st_io = nullptr;
+    void* arena_base = nullptr;
+    Arena arena;
+    BatchCase* d_cases = nullptr;
+    BatchCase* h_cases = nullptr; // host scratch, one entry per slot (uploaded through case_stage)
+    ChunkState* d_chunk = nullptr;
+    BatchTile* d_tiles = nullptr;
+    size_t tiles_cap = 0;
+    int* d_counters = nullptr;
+    Staging chunk_stage[kRing], tile_stage[kRing], case_stage[kRing];
+    int chunk_ring = 0, tile_ring = 0, case_ring = 0;
+    cudaGraphExec_t exec = nullptr;
+    int graph_ntiles = 0;
+    bool composition_dirty = true;
+    std::vector<int64_t> slot_req;   // request id per slot, or 0
+    std::deque<cudaEvent_t> inflight; // one event per replay in flight
+    std::vector<cudaEvent_t> event_pool;
+    cudaEvent_t t0_ev = nullptr;
+    std::chrono::steady_clock::time_point t0;
+    // cost model of a tile: (planes + tile_ovh) x plane_ns[kind]; measured by calibrate()
+    double plane_ns[BK_COUNT] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
+    double tile_ovh = 3.0;
+    int last_z = 0; // tile depth the planner chose for the current composition
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<int64_t> pending;
+    std::map<int64_t, std::unique_ptr<Request>> reqs;
+    int64_t next_id = 1;
+    bool stopping = false;
+    std::string fatal;
+    std::thread worker;
+
+    // statistics
+    int64_t submitted = 0, completed = 0, failed = 0, node_updates = 0, compositions = 0, replays = 0;
+    double first_admit = -1, last_done = -1;
+
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+size_t footprint(const mbcg_params& p, long long* pitch, long long* fstride, int* es, int* nparts) {
+    *es = p.precision == MBCG_FP32 ? 4 : 2;
+    *pitch = (p.nx + 7) / 8 * 8;
+    const long long per_field = *pitch * p.ny * p.nz;
+    *fstride = static_cast<long long>(align_up(static_cast<size_t>(per_field * *es), kAlign)) / *es;
+    StepParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.nx = p.nx;
+    P.ny = p.ny;
+    P.nz = p.nz;
+    *nparts = diag_partials_needed(P);
+    const size_t states = 2ull * NF * static_cast<size_t>(*fstride) * *es;
+    const size_t diag = align_up(sizeof(double) * kDiagSlots * (*nparts + 1) + 16, kAlign);
+    return states + diag;
+}
+
+StepParams step_params(const Request& r, int from, int* status_word) {
+    StepParams P;
+    fill_step_physics(r.p, P);
+    P.pitch = r.pitch;
+    P.plane = r.plane;
+    P.zchunk = r.zchunk;
+    P.status = status_word;
+    P.step = 0;
+    for (int i = 0; i < NF; ++i) {
+        P.a[i] = r.fields[from][i];
+        P.b[i] = r.fields[from ^ 1][i];
+    }
+    return P;
+}
+
+cudaEvent_t take_event(mbcg_server* s) {
+    if (!s->event_pool.empty()) {
+        cudaEvent_t e = s->event_pool.back();
+        s->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    return e;
+}
+
+// Pinned staging buffer of at least n bytes whose previous copy has executed.
+cudaError_t stage(Staging* ring, int* idx, size_t n, Staging** out) {
+    Staging& b = ring[*idx];
+    *idx = (*idx + 1) % kRing;
+    if (b.pending) {
+        cudaError_t e = cudaEventSynchronize(b.ev);
+        if (e != cudaSuccess) return e;
+        b.pending = false;
+    }
+    if (b.cap < n) {
+        if (b.host) cudaFreeHost(b.host);
+        b.host = nullptr;
+        b.cap = 0;
+        cudaError_t e = cudaMallocHost(&b.host, std::max(n, static_cast<size_t>(4096)));
+        if (e != cudaSuccess) return e;
+        b.cap = std::max(n, static_cast<size_t>(4096));
+    }
+    if (!b.ev) {
+        cudaError_t e = cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
+    *out = &b;
+    return cudaSuccess;
+}
+
+cudaError_t upload(mbcg_server* s, Staging* ring, int* idx, void* dst, const void* src, size_t n) {
+    Staging* b = nullptr;
+    cudaError_t e = stage(ring, idx, n, &b);
+    if (e != cudaSuccess) return e;
+    std::memcpy(b->host, src, n);
+    e = cudaMemcpyAsync(dst, b->host, n, cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev, s->st);
+    if (e == cudaSuccess) b->pending = true;
+    return e;
+}
+
+int live_count(const mbcg_server* s) {
+    int n = 0;
+    for (int64_t id : s->slot_req) n += id != 0;
+    return n;
+}
+
+// ---------------------------------------------------------------- admission
+// Called with the mutex held.  Returns a CUDA error (the server then fails).
+cudaError_t admit(mbcg_server* s, Request& r, int slot) {
+    int nparts = 0;
+    r.bytes = footprint(r.p, &r.pitch, &r.fstride, &r.es, &nparts);
+    r.plane = r.pitch * r.p.ny;
+    r.nparts = nparts;
+    unsigned char* base = static_cast<unsigned char*>(s->arena_base) + r.off;
+    for (int st = 0; st < 2; ++st)
+        for (int i = 0; i < NF; ++i)
+            r.fields[st][i] = base + (static_cast<size_t>(st) * NF + i) * static_cast<size_t>(r.fstride) * r.es;
+    unsigned char* dbase = base + 2ull * NF * static_cast<size_t>(r.fstride) * r.es;
+    r.d_result = reinterpret_cast<double*>(dbase);
+    r.d_partials = r.d_result + kDiagSlots + 2;
+    int* status_word = reinterpret_cast<int*>(r.d_result + kDiagSlots + 1);
+    r.nodes = static_cast<int64_t>(r.p.nx - 2) * (r.p.ny - 2) * (r.p.nz - 2);
+    r.slot = slot;
+    r.cur = 0;
+    r.resident = true;
+    {
+        StepParams P0;
+        fill_step_physics(r.p, P0);
+        r.features = features_of(P0);
+    }
+    r.zchunk = r.p.nz - 2; // set per composition by the planner (rebuild)
+
+    // lattice table entry (host side; rebuild() uploads the table of the composition)
+    BatchCase& C = s->h_cases[slot];
+    std::memset(&C, 0, sizeof(C));
+    for (int par = 0; par < 2; ++par) {
+        C.P[par] = step_params(r, par, status_word);
+        const void* f[NF];
+        for (int i = 0; i < NF; ++i) f[i] = r.fields[par][i];
+        if (encode_state_maps(r.p, f, r.pitch, kBatchW, *reinterpret_cast<TensorMaps*>(C.maps[par])) != MBCG_OK)
+            return cudaErrorInvalidValue;
+    }
+    C.kind = batch_kind(r.p.q, r.p.precision, r.features);
+    // a clean state (every byte the case can read is its own) and its initial condition
+    cudaError_t e = cudaMemsetAsync(base, 0, r.bytes, s->st);
+    if (e == cudaSuccess) {
+        StepParams P = step_params(r, 1, status_word); // P.b = state 0
+        e = launch_init(r.p.precision, P, r.p, s->st);
+    }
+    if (e != cudaSuccess) return e;
+    r.state = MBCG_REQ_RUNNING;
+    r.t_admit = s->now();
+    if (s->first_admit < 0) s->first_admit = r.t_admit;
+    s->slot_req[slot] = r.id;
+    s->composition_dirty = true;
+    return cudaSuccess;
+}
+
+// tiles of a lattice at the reference depth of 16 planes (the admission measure of load)
+long long load_tiles(const mbcg_params& p) {
+    const long long gx = (p.nx - 2 + kStepTileX - 1) / kStepTileX;
+    const long long gy = (p.ny - 2 + step_tile_rows(kBatchW) - 1) / step_tile_rows(kBatchW);
+    return gx * gy * ((p.nz - 2 + 15) / 16);
+}
+
+// Admission.  FIFO: arrival order.  Shortest job first: ascending estimated remaining time,
+// where a request's wait counts against its work at the server's throughput (aging), so a
+// large request is not passed over forever.  Under shortest job first the live set stops
+// growing once its tiles fill cfg.fill_waves waves of the SMs: more lattices would not raise
+// the throughput, only share it and delay every completion.
+cudaError_t admit_pending(mbcg_server* s) {
+    if (s->pending.empty()) return cudaSuccess;
+    std::vector<int64_t> order(s->pending.begin(), s->pending.end());
+    const bool sjf = s->cfg.policy == MBCG_POLICY_SJF;
+    if (sjf) {
+        // node updates per second of the GPU under the cost model (D3Q27 FP32 body)
+        const double rate = s->nsm * static_cast<double>(kStepTileX * step_tile_rows(kBatchW)) /
+                            (s->plane_ns[BK_Q27_F32] * 1e-9);
+        const double now = s->now();
+        auto key = [&](int64_t id) {
+            const Request& r = *s->reqs.at(id);
+            return static_cast<double>(r.nodes_estimate()) * static_cast<double>(r.steps) / rate - (now - r.t_submit);
+        };
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key(a) < key(b); });
+    }
+    long long live_tiles = 0;
+    for (int64_t id : s->slot_req)
+        if (id) live_tiles += load_tiles(s->reqs.at(id)->p);
+    const long long fill = static_cast<long long>(std::max(1, s->cfg.fill_waves)) * s->nsm;
+    std::vector<int64_t> admitted;
+    for (int64_t id : order) {
+        if (sjf && live_tiles >= fill) break;
+        int slot = -1;
+        for (int i = 0; i < s->cfg.max_live; ++i)
+            if (s->slot_req[i] == 0) {
+                slot = i;
+                break;
+            }
+        if (slot < 0) break;
+        Request& r = *s->reqs.at(id);
+        long long pitch, fstride;
+        int es, nparts;
+        const size_t need = footprint(r.p, &pitch, &fstride, &es, &nparts);
+        size_t off = 0;
+        if (s->arena.alloc(need, &off)) {
+            r.off = off;
+            cudaError_t e = admit(s, r, slot);
+            if (e != cudaSuccess) return e;
+            admitted.push_back(id);
+            live_tiles += load_tiles(r.p);
+        } else if (!s->cfg.backfill) {
+            break;
+        }
+    }
+    for (int64_t id : admitted) s->pending.erase(std::find(s->pending.begin(), s->pending.end(), id));
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------- composition and graph
+struct TileItem {
+    BatchTile t;
+    int kind;
+    double cost; // predicted ns
+};
+
+// Tiles of every live lattice for a target depth z: each lattice's z axis is cut into equal
+// chunks of at most z planes; a tile costs (planes + 2 warm-up planes + overhead) x the
+// calibrated time of one plane of its kernel body.
+void make_tiles(const mbcg_server* s, int z, std::vector<TileItem>& items, std::vector<int>& zc) {
+    items.clear();
+    zc.assign(s->cfg.max_live, 0);
+    for (int slot = 0; slot < s->cfg.max_live; ++slot) {
+        const int64_t id = s->slot_req[slot];
+        if (!id) continue;
+        const Request& r = *s->reqs.at(id);
+        const int gx = (r.p.nx - 2 + kStepTileX - 1) / kStepTileX;
+        const int gy = (r.p.ny - 2 + step_tile_rows(kBatchW) - 1) / step_tile_rows(kBatchW);
+        const int nzf = r.p.nz - 2;
+        const int nch = std::max(1, (nzf + z - 1) / z);
+        const int depth = (nzf + nch - 1) / nch;
+        const int gz = (nzf + depth - 1) / depth;
+        zc[slot] = depth;
+        const int kind = batch_kind(r.p.q, r.p.precision, r.features);
+        for (int bz = 0; bz < gz; ++bz) {
+            const double planes = std::min(depth, nzf - bz * depth) + 2 + s->tile_ovh;
+            for (int by = 0; by < gy; ++by)
+                for (int bx = 0; bx < gx; ++bx)
+                    items.push_back({BatchTile{static_cast<uint16_t>(slot), static_cast<uint16_t>(bx),
+                                               static_cast<uint16_t>(by), static_cast<uint16_t>(bz)},
+                                     kind, planes * s->plane_ns[kind]});
+        }
+    }
+    // longest tiles first: the atomic queue then runs a greedy longest-processing-time schedule
+    std::stable_sort(items.begin(), items.end(), [](const TileItem& a, const TileItem& b) {
+        if (a.cost != b.cost) return a.cost > b.cost;
+        return a.kind < b.kind;
+    });
+}
+
+// Predicted duration of one launch: the greedy schedule of the sorted tiles on nsm CTAs.
+double predict_ns(const std::vector<TileItem>& items, int nsm) {
+    std::vector<double> load(std::max(1, nsm), 0.0);
+    std::make_heap(load.begin(), load.end(), std::greater<double>());
+    for (const TileItem& it : items) {
+        std::pop_heap(load.begin(), load.end(), std::greater<double>());
+        load.back() += it.cost;
+        std::push_heap(load.begin(), load.end(), std::greater<double>());
+    }
+    return *std::max_element(load.begin(), load.end());
+}
+
+cudaError_t rebuild(mbcg_server* s) {
+    // planner: the tile depth with the shortest predicted launch (fixed if configured)
+    std::vector<TileItem> items, best_items;
+    std::vector<int> zc, best_zc;
+    int best_z = s->cfg.zchunk;
+    if (best_z > 0) {
+        make_tiles(s, best_z, best_items, best_zc);
+    } else {
+        double best = 1e300;
+        for (int z : {8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 512}) {
+            make_tiles(s, z, items, zc);
+            const double t = predict_ns(items, s->nsm);
+            if (t < best * 0.999) {
+                best = t;
+                best_z = z;
+                best_items.swap(items);
+                best_zc.swap(zc);
+            }
+        }
+    }
+    s->last_z = best_z;
+    // lattice table with this composition's depths
+    for (int slot = 0; slot < s->cfg.max_live; ++slot) {
+        if (!s->slot_req[slot]) continue;
+        Request& r = *s->reqs.at(s->slot_req[slot]);
+        r.zchunk = best_zc[slot];
+        s->h_cases[slot].P[0].zchunk = r.zchunk;
+        s->h_cases[slot].P[1].zchunk = r.zchunk;
+    }
+    cudaError_t e = upload(s, s->case_stage, &s->case_ring, s->d_cases, s->h_cases,
+                           sizeof(BatchCase) * s->cfg.max_live);
+    if (e != cudaSuccess) return e;
+    std::vector<BatchTile> tiles(best_items.size());
+    for (size_t i = 0; i < best_items.size(); ++i) tiles[i] = best_items[i].t;
+    const int ntiles = static_cast<int>(tiles.size());
+    if (static_cast<size_t>(ntiles) > s->tiles_cap) {
+        // the old queue may still be read by a replay in flight
+        e = cudaStreamSynchronize(s->st);
+        if (e != cudaSuccess) return e;
+        if (s->d_tiles) cudaFree(s->d_tiles);
+        s->d_tiles = nullptr;
+        s->tiles_cap = std::max<size_t>(ntiles, 2 * s->tiles_cap);
+        e = cudaMalloc(&s->d_tiles, s->tiles_cap * sizeof(BatchTile));
+        if (e != cudaSuccess) return e;
+    }
+    if (ntiles > 0) {
+        e = upload(s, s->tile_stage, &s->tile_ring, s->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile));
+        if (e != cudaSuccess) return e;
+    }
+    // capture: reset the per-launch counters, then chunk_steps launches
+    const int grid = std::max(1, std::min(ntiles, s->nsm));
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    cudaError_t ec = cudaMemsetAsync(s->d_counters, 0, sizeof(int) * s->cfg.chunk_steps, s->st);
+    for (int j = 0; j < s->cfg.chunk_steps && ec == cudaSuccess; ++j)
+        ec = launch_batch(s->d_cases, s->d_tiles, ntiles, s->d_chunk, s->d_counters, j, grid, s->st);
+    e = cudaStreamEndCapture(s->st, &g);
+    if (ec != cudaSuccess) e = ec;
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return e;
+    }
+    if (s->exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(s->exec, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(s->exec);
+            s->exec = nullptr;
+        }
+    }
+    if (!s->exec) e = cudaGraphInstantiate(&s->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return e;
+    s->graph_ntiles = ntiles;
+    s->composition_dirty = false;
+    s->compositions += 1;
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------- one replay
+cudaError_t run_chunk(mbcg_server* s, std::unique_lock<std::mutex>& lk) {
+    const int K = s->cfg.chunk_steps;
+    std::vector<ChunkState> cs(s->cfg.max_live);
+    for (int slot = 0; slot < s->cfg.max_live; ++slot) {
+        cs[slot] = ChunkState{0, 0, 0};
+        const int64_t id = s->slot_req[slot];
+        if (!id) continue;
+        const Request& r = *s->reqs.at(id);
+        cs[slot] = ChunkState{r.steps_done, r.cur, static_cast<int>(std::min<int64_t>(K, r.steps - r.steps_done))};
+    }
+    cudaError_t e = upload(s, s->chunk_stage, &s->chunk_ring, s->d_chunk, cs.data(), cs.size() * sizeof(ChunkState));
+    if (e == cudaSuccess && s->graph_ntiles > 0) e = cudaGraphLaunch(s->exec, s->st);
+    if (e != cudaSuccess) return e;
+    s->replays += 1;
+    cudaEvent_t ev = take_event(s);
+    e = cudaEventRecord(ev, s->st);
+    if (e != cudaSuccess) return e;
+    s->inflight.push_back(ev);
+    // exact host bookkeeping; retire the lattices this replay finishes
+    for (int slot = 0; slot < s->cfg.max_live; ++slot) {
+        const int64_t id = s->slot_req[slot];
+        if (!id) continue;
+        Request& r = *s->reqs.at(id);
+        const int n = cs[slot].nsteps;
+        r.steps_done += n;
+        r.cur ^= (n & 1);
+        s->node_updates += static_cast<int64_t>(n) * r.nodes;
+        if (r.steps_done >= r.steps) {
+            StepParams P = step_params(r, r.cur, nullptr);
+            e = launch_diag(r.p.precision, P, r.p, r.d_partials, r.nparts, r.d_result, s->st);
+            if (e == cudaSuccess)
+                e = launch_state_hash(r.p.precision, P, reinterpret_cast<unsigned long long*>(r.d_result + kDiagSlots),
+                                      s->st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(r.h_result, r.d_result, sizeof(double) * (kDiagSlots + 2), cudaMemcpyDeviceToHost,
+                                    s->st);
+            if (e != cudaSuccess) return e;
+            r.done_ev = nullptr;
+            e = cudaEventCreate(&r.done_ev);
+            if (e == cudaSuccess) e = cudaEventRecord(r.done_ev, s->st);
+            if (e != cudaSuccess) return e;
+            r.retiring = true;
+            s->slot_req[slot] = 0;
+            s->composition_dirty = true;
+        }
+    }
+    (void)lk;
+    return cudaSuccess;
+}
+
+// Completion of retiring lattices.  Mutex held.
+void reap(mbcg_server* s) {
+    bool any = false;
+    for (auto& kv : s->reqs) {
+        Request& r = *kv.second;
+        if (!r.retiring) continue;
+        const cudaError_t q = cudaEventQuery(r.done_ev);
+        if (q == cudaErrorNotReady) continue;
+        r.retiring = false;
+        if (q != cudaSuccess) {
+            r.state = MBCG_REQ_FAILED;
+            s->fatal = std::string("lattice completion: ") + cudaGetErrorString(q);
+        } else {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, s->t0_ev, r.done_ev);
+            r.t_done = ms * 1e-3;
+            const double* h = r.h_result;
+            r.diag.mass_r = h[0];
+            r.diag.mass_b = h[1];
+            for (int a = 0; a < 3; ++a) r.diag.momentum[a] = h[2 + a];
+            r.diag.p_in = h[6] > 0 ? h[5] / h[6] : 0.0;
+            r.diag.p_out = h[8] > 0 ? h[7] / h[8] : 0.0;
+            r.diag.dp = r.diag.p_in - r.diag.p_out;
+            r.diag.nonfinite = static_cast<int64_t>(h[9]);
+            r.diag.nodes = static_cast<int64_t>(h[10]);
+            std::memcpy(&r.hash, &h[kDiagSlots], sizeof(uint64_t));
+            int st = 0;
+            std::memcpy(&st, &h[kDiagSlots + 1], sizeof(int));
+            r.status = st;
+            r.state = st == 0 ? MBCG_REQ_DONE : MBCG_REQ_FAILED;
+        }
+        cudaEventDestroy(r.done_ev);
+        r.done_ev = nullptr;
+        if (r.state == MBCG_REQ_DONE) s->completed += 1;
+        else s->failed += 1;
+        s->last_done = std::max(s->last_done, r.t_done);
+        if (!s->cfg.keep_results || r.state != MBCG_REQ_DONE) {
+            s->arena.release(r.off, r.bytes);
+            r.resident = false;
+        }
+        any = true;
+    }
+    if (any) s->cv_done.notify_all();
+}
+
+void fail_all(mbcg_server* s, const std::string& msg) {
+    s->fatal = msg;
+    for (auto& kv : s->reqs) {
+        Request& r = *kv.second;
+        if (r.state == MBCG_REQ_QUEUED || r.state == MBCG_REQ_RUNNING) {
+            r.state = MBCG_REQ_FAILED;
+            s->failed += 1;
+        }
+    }
+    s->pending.clear();
+    s->cv_done.notify_all();
+}
+
+void worker_main(mbcg_server* s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        if (!s->fatal.empty() || s->stopping) break;
+        reap(s);
+        cudaError_t e = admit_pending(s);
+        if (e != cudaSuccess) {
+            fail_all(s, std::string("admission: ") + cudaGetErrorString(e));
+            break;
+        }
+        const int live = live_count(s);
+        bool retiring = false;
+        for (auto& kv : s->reqs) retiring |= kv.second->retiring;
+        if (live == 0) {
+            if (retiring || !s->inflight.empty()) {
+                // nothing to launch: wait for the GPU to finish what is queued
+                cudaEvent_t ev = s->inflight.empty() ? nullptr : s->inflight.front();
+                lk.unlock();
+                if (ev) cudaEventSynchronize(ev);
+                else cudaStreamSynchronize(s->st);
+                lk.lock();
+                if (ev && !s->inflight.empty() && s->inflight.front() == ev) {
+                    s->inflight.pop_front();
+                    s->event_pool.push_back(ev);
+                }
+                continue;
+            }
+            s->cv_work.wait_for(lk, std::chrono::milliseconds(20));
+            continue;
+        }
+        if (s->composition_dirty) {
+            e = rebuild(s);
+            if (e != cudaSuccess) {
+                fail_all(s, std::string("batch graph: ") + cudaGetErrorString(e));
+                break;
+            }
+        }
+        e = run_chunk(s, lk);
+        if (e != cudaSuccess) {
+            fail_all(s, std::string("batch replay: ") + cudaGetErrorString(e));
+            break;
+        }
+        // at most two replays in flight
+        while (s->inflight.size() > 2) {
+            cudaEvent_t ev = s->inflight.front();
+            lk.unlock();
+            e = cudaEventSynchronize(ev);
+            lk.lock();
+            s->inflight.pop_front();
+            s->event_pool.push_back(ev);
+            if (e != cudaSuccess) {
+                fail_all(s, std::string("batch replay: ") + cudaGetErrorString(e));
+                break;
+            }
+        }
+    }
+    // drain what is in flight; lattices still running when the server stops fail
+    lk.unlock();
+    cudaStreamSynchronize(s->st);
+    lk.lock();
+    reap(s);
+    for (cudaEvent_t ev : s->inflight) s->event_pool.push_back(ev);
+    s->inflight.clear();
+    for (int64_t& id : s->slot_req) {
+        if (!id) continue;
+        Request& r = *s->reqs.at(id);
+        r.state = MBCG_REQ_FAILED;
+        s->failed += 1;
+        id = 0;
+    }
+    s->cv_done.notify_all();
+}
+
+// Calibration of the planner's cost model.  For each kernel body, one synthetic lattice whose
+// tile grid per z chunk is exactly one CTA per SM (8 x nsm/8 tiles) is stepped with deep
+// (128-plane) and shallow (16-plane) tiles: t_deep = (130 + o) c and t_shallow = 8 (18 + o) c
+// give the time c of one tile plane and the fixed cost o of a tile in planes.
+cudaError_t time_launches(mbcg_server* s, int ntiles, int reps, float* ms) {
+    ChunkState cs{0, 0, 1 << 20};
+    cudaError_t e = cudaMemcpyAsync(s->d_chunk, &cs, sizeof(cs), cudaMemcpyHostToDevice, s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_counters, 0, sizeof(int) * (reps + 1), s->st);
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    const int grid = std::min(ntiles, s->nsm);
+    if (e == cudaSuccess) e = launch_batch(s->d_cases, s->d_tiles, ntiles, s->d_chunk, s->d_counters, 0, grid, s->st);
+    if (e == cudaSuccess) e = cudaEventRecord(a, s->st);
+    for (int j = 1; j <= reps && e == cudaSuccess; ++j)
+        e = launch_batch(s->d_cases, s->d_tiles, ntiles, s->d_chunk, s->d_counters, j, grid, s->st);
+    if (e == cudaSuccess) e = cudaEventRecord(b, s->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, a, b);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    return e;
+}
+
+int calibrate(mbcg_server* s) {
+    if (s->nsm % 8 != 0) return MBCG_OK; // keep the default model
+    const int gx = 8, gy = s->nsm / 8;
+    const int reps = 4;
+    double ovh_sum = 0.0;
+    int ovh_n = 0;
+    for (int kind = 0; kind < BK_COUNT; ++kind) {
+        const bool lean = kind >= BK_Q19_F32_P;
+        int q, prec;
+        if (!lean) {
+            q = kind >= BK_Q27_F32 ? 27 : 19;
+            prec = kind % 3;
+        } else {
+            q = kind >= BK_Q27_F32_P ? 27 : 19;
+            prec = (kind - BK_Q19_F32_P) % 2;
+        }
+        mbcg_params p;
+        mbcg_params_default(&p);
+        p.q = q;
+        p.precision = prec;
+        p.nx = 2 + gx * kStepTileX;
+        p.ny = 2 + gy * step_tile_rows(kBatchW);
+        p.nz = 2 + 128;
+        p.bc[0] = p.bc[1] = p.bc[2] = MBCG_BC_PERIODIC;
+        p.ic = MBCG_IC_BUBBLE;
+        p.bubble_radius = 40;
+        p.bubble_width = 3;
+        p.bubble_phase = 1;
+        p.bubble_center[0] = 0.5 * (p.nx - 1);
+        p.bubble_center[1] = 0.5 * (p.ny - 1);
+        p.bubble_center[2] = 0.5 * (p.nz - 1);
+        p.tau = 0.8;
+        p.sigma = 0.01;
+        p.beta = 0.7;
+        if (!lean) p.gravity[2] = -1e-9; // a forced lattice runs the body with every feature
+        Request r;
+        r.p = p;
+        r.id = -1;
+        long long pitch, fstride;
+        int es, nparts;
+        r.bytes = footprint(p, &pitch, &fstride, &es, &nparts);
+        if (!s->arena.alloc(r.bytes, &r.off)) return fail(MBCG_E_NOMEM, "arena too small to calibrate");
+        const int64_t saved = s->slot_req[0];
+        cudaError_t e = admit(s, r, 0);
+        s->slot_req[0] = saved;
+        if (e == cudaSuccess && batch_kind(q, prec, r.features) != kind) e = cudaErrorInvalidValue;
+        float t[2] = {0, 0};
+        for (int d = 0; d < 2 && e == cudaSuccess; ++d) {
+            const int depth = d == 0 ? 128 : 16;
+            BatchCase& C = s->h_cases[0];
+            C.P[0].zchunk = C.P[1].zchunk = depth;
+            e = cudaMemcpyAsync(s->d_cases, &C, sizeof(C), cudaMemcpyHostToDevice, s->st);
+            std::vector<BatchTile> tiles;
+            for (int bz = 0; bz < 128 / depth; ++bz)
+                for (int by = 0; by < gy; ++by)
+                    for (int bx = 0; bx < gx; ++bx)
+                        tiles.push_back(BatchTile{0, static_cast<uint16_t>(bx), static_cast<uint16_t>(by),
+                                                  static_cast<uint16_t>(bz)});
+            if (e == cudaSuccess && tiles.size() > s->tiles_cap) {
+                e = cudaStreamSynchronize(s->st);
+                if (s->d_tiles) cudaFree(s->d_tiles);
+                s->d_tiles = nullptr;
+                s->tiles_cap = std::max<size_t>(tiles.size(), 65536);
+                if (e == cudaSuccess) e = cudaMalloc(&s->d_tiles, s->tiles_cap * sizeof(BatchTile));
+            }
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(s->d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
+                                    s->st);
+            float ms = 0.0f;
+            if (e == cudaSuccess) e = time_launches(s, static_cast<int>(tiles.size()), reps, &ms);
+            t[d] = ms * 1e6f / reps; // ns per launch
+        }
+        cudaError_t es2 = cudaStreamSynchronize(s->st);
+        if (e == cudaSuccess) e = es2;
+        s->arena.release(r.off, r.bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "calibration");
+        // t0 = (130 + o) c, t1 = 8 (18 + o) c  =>  o = (130 t1 - 144 t0) / (8 t0 - t1)
+        const double t0 = t[0], t1 = t[1];
+        double o = (8.0 * t0 - t1) != 0.0 ? (130.0 * t1 - 144.0 * t0) / (8.0 * t0 - t1) : 3.0;
+        o = std::min(std::max(o, 0.0), 32.0);
+        s->plane_ns[kind] = t0 / (130.0 + o);
+        ovh_sum += o;
+        ovh_n += 1;
+    }
+    if (ovh_n) s->tile_ovh = ovh_sum / ovh_n;
+    s->first_admit = -1;
+    s->composition_dirty = true;
+    return MBCG_OK;
+}
+
+void destroy_server(mbcg_server* s) {
+    if (!s) return;
+    if (s->worker.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stopping = true;
+            s->pending.clear();
+        }
+        s->cv_work.notify_all();
+        s->worker.join();
+    }
+    if (s->st) cudaStreamSynchronize(s->st);
+    for (auto& kv : s->reqs) {
+        if (kv.second->done_ev) cudaEventDestroy(kv.second->done_ev);
+        if (kv.second->h_result) cudaFreeHost(kv.second->h_result);
+    }
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    for (Staging* ring : {s->chunk_stage, s->tile_stage, s->case_stage})
+        for (int i = 0; i < kRing; ++i) {
+            if (ring[i].host) cudaFreeHost(ring[i].host);
+            if (ring[i].ev) cudaEventDestroy(ring[i].ev);
+        }
+    for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : s->inflight) cudaEventDestroy(e);
+    if (s->t0_ev) cudaEventDestroy(s->t0_ev);
+    if (s->d_tiles) cudaFree(s->d_tiles);
+    if (s->d_chunk) cudaFree(s->d_chunk);
+    if (s->d_counters) cudaFree(s->d_counters);
+    if (s->d_cases) cudaFree(s->d_cases);
+    std::free(s->h_cases);
+    if (s->arena_base) cudaFree(s->arena_base);
+    if (s->st) cudaStreamDestroy(s->st);
+    if (s->st_io) cudaStreamDestroy(s->st_io);
+    delete s;
+}
+
+void fill_info(const Request& r, mbcg_request_info* out) {
+    std::memset(out, 0, sizeof(*out));
+    out->id = r.id;
+    out->state = r.state;
+    out->status = r.status;
+    out->steps = r.steps;
+    out->steps_done = r.state == MBCG_REQ_DONE ? r.steps : std::min(r.steps_done, r.steps);
+    out->t_submit = r.t_submit;
+    out->t_admit = r.t_admit;
+    out->t_done = r.state == MBCG_REQ_DONE || r.state == MBCG_REQ_FAILED ? r.t_done : -1.0;
+    out->state_hash = r.hash;
+    out->diag = r.diag;
+}
+
+} // namespace
+
+extern "C" {
+
+void mbcg_server_config_default(mbcg_server_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->max_live = 64;
+    cfg->chunk_steps = 16;
+    cfg->backfill = 1;
+    cfg->calibrate = 1;
+    cfg->policy = MBCG_POLICY_FIFO;
+    cfg->fill_waves = 4;
+}
+
+int mbcg_server_create(const mbcg_server_config* cfg_in, mbcg_server** out) {
+    if (!out) return fail(MBCG_E_INVALID, "null output handle");
+    *out = nullptr;
+    mbcg_server_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else mbcg_server_config_default(&cfg);
+    if (cfg.max_live <= 0) cfg.max_live = 64;
+    if (cfg.max_live > kMaxLiveCap) return fail(MBCG_E_INVALID, "max_live above 4096");
+    if (cfg.chunk_steps <= 0) cfg.chunk_steps = 16;
+    if (cfg.chunk_steps > 1024) return fail(MBCG_E_INVALID, "chunk_steps above 1024");
+    if (cfg.zchunk < 0) return fail(MBCG_E_INVALID, "negative zchunk");
+    if (cfg.policy != MBCG_POLICY_FIFO && cfg.policy != MBCG_POLICY_SJF) return fail(MBCG_E_INVALID, "unknown policy");
+    if (cfg.fill_waves <= 0) cfg.fill_waves = 4;
+    auto* s = new mbcg_server();
+    s->cfg = cfg;
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st_io, cudaStreamNonBlocking);
+    size_t arena = static_cast<size_t>(cfg.arena_bytes);
+    if (e == cudaSuccess && arena == 0) {
+        size_t fr = 0, tot = 0;
+        e = cudaMemGetInfo(&fr, &tot);
+        arena = static_cast<size_t>(0.7 * static_cast<double>(fr));
+    }
+    arena = arena / kAlign * kAlign;
+    if (e == cudaSuccess) e = cudaMalloc(&s->arena_base, arena);
+    if (e != cudaSuccess) {
+        const int rc = e == cudaErrorMemoryAllocation ? fail(MBCG_E_NOMEM, "server arena allocation failed")
+                                                      : cuda_fail(e, "mbcg_server_create");
+        destroy_server(s);
+        return rc;
+    }
+    s->arena.reset(arena);
+    s->cfg.arena_bytes = static_cast<int64_t>(arena);
+    s->slot_req.assign(cfg.max_live, 0);
+    e = cudaMalloc(&s->d_cases, sizeof(BatchCase) * cfg.max_live);
+    if (e == cudaSuccess) {
+        s->h_cases = static_cast<BatchCase*>(std::calloc(cfg.max_live, sizeof(BatchCase)));
+        if (!s->h_cases) e = cudaErrorMemoryAllocation;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_chunk, sizeof(ChunkState) * cfg.max_live);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_counters, sizeof(int) * std::max(cfg.chunk_steps, 8));
+    if (e == cudaSuccess) {
+        s->tiles_cap = 65536;
+        e = cudaMalloc(&s->d_tiles, s->tiles_cap * sizeof(BatchTile));
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_chunk, 0, sizeof(ChunkState) * cfg.max_live, s->st);
+    // opt the batch kernel into its shared memory outside any capture
+    if (e == cudaSuccess) e = launch_batch(s->d_cases, nullptr, 0, s->d_chunk, s->d_counters, 0, 0, s->st);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->t0_ev);
+    if (e == cudaSuccess) e = cudaEventRecord(s->t0_ev, s->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(s->t0_ev);
+    s->t0 = std::chrono::steady_clock::now();
+    if (e != cudaSuccess) {
+        const int rc = cuda_fail(e, "mbcg_server_create");
+        destroy_server(s);
+        return rc;
+    }
+    if (cfg.calibrate && cfg.zchunk == 0) {
+        if (int rc = calibrate(s)) {
+            destroy_server(s);
+            return rc;
+        }
+    }
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return MBCG_OK;
+}
+
+int mbcg_server_destroy(mbcg_server* s) {
+    destroy_server(s);
+    return MBCG_OK;
+}
+
+int mbcg_server_submit(mbcg_server* s, const mbcg_params* p, int64_t nsteps, int64_t* id) {
+    if (!s || !id) return fail(MBCG_E_INVALID, "null argument");
+    if (int rc = validate_params(p)) return rc;
+    if (nsteps < 0) return fail(MBCG_E_INVALID, "negative step count");
+    if (p->ic == MBCG_IC_NONE) return fail(MBCG_E_INVALID, "a served case needs an initial condition");
+    if (p->nx - 2 > 0xffff * kStepTileX || p->ny - 2 > 0xffff * step_tile_rows(kBatchW) || p->nz - 2 > 0xffff * 8)
+        return fail(MBCG_E_UNSUPPORTED, "lattice too large for the tile queue");
+    long long pitch, fstride;
+    int es, nparts;
+    const size_t need = footprint(*p, &pitch, &fstride, &es, &nparts);
+    if (need > s->arena.size()) return fail(MBCG_E_NOMEM, "lattice larger than the server arena");
+    auto r = std::make_unique<Request>();
+    r->p = *p;
+    r->steps = nsteps;
+    if (cudaMallocHost(&r->h_result, sizeof(double) * (kDiagSlots + 2)) != cudaSuccess)
+        return fail(MBCG_E_NOMEM, "pinned result buffer");
+    std::memset(r->h_result, 0, sizeof(double) * (kDiagSlots + 2));
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (!s->fatal.empty()) {
+            cudaFreeHost(r->h_result);
+            return fail(MBCG_E_CUDA, "server failed: " + s->fatal);
+        }
+        r->id = s->next_id++;
+        r->t_submit = s->now();
+        *id = r->id;
+        s->pending.push_back(r->id);
+        s->reqs[r->id] = std::move(r);
+        s->submitted += 1;
+    }
+    s->cv_work.notify_all();
+    return MBCG_OK;
+}
+
+int mbcg_server_poll(mbcg_server* s, int64_t id, mbcg_request_info* out) {
+    if (!s || !out) return fail(MBCG_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return fail(MBCG_E_INVALID, "unknown request id");
+    fill_info(*it->second, out);
+    return MBCG_OK;
+}
+
+int mbcg_server_wait(mbcg_server* s, int64_t id, double timeout_s, mbcg_request_info* out) {
+    if (!s) return fail(MBCG_E_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return fail(MBCG_E_INVALID, "unknown request id");
+    Request& r = *it->second;
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+    while (r.state != MBCG_REQ_DONE && r.state != MBCG_REQ_FAILED) {
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout &&
+            r.state != MBCG_REQ_DONE && r.state != MBCG_REQ_FAILED)
+            return fail(MBCG_E_TIMEOUT, "request not finished within the timeout");
+    }
+    if (out) fill_info(r, out);
+    return MBCG_OK;
+}
+
+int mbcg_server_drain(mbcg_server* s, double timeout_s) {
+    if (!s) return fail(MBCG_E_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+    auto busy = [&] {
+        for (auto& kv : s->reqs)
+            if (kv.second->state == MBCG_REQ_QUEUED || kv.second->state == MBCG_REQ_RUNNING) return true;
+        return false;
+    };
+    while (busy()) {
+        if (!s->fatal.empty()) return fail(MBCG_E_CUDA, "server failed: " + s->fatal);
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && busy())
+            return fail(MBCG_E_TIMEOUT, "server not drained within the timeout");
+    }
+    return MBCG_OK;
+}
+
+int mbcg_server_fetch(mbcg_server* s, int64_t id, float* const host[MBCG_NFIELDS]) {
+    if (!s || !host) return fail(MBCG_E_INVALID, "null argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return fail(MBCG_E_INVALID, "unknown request id");
+    Request& r = *it->second;
+    if (r.state != MBCG_REQ_DONE || !r.resident)
+        return fail(MBCG_E_INVALID, "request has no resident result (not done, released, or keep_results off)");
+    StepParams P = step_params(r, r.cur, nullptr);
+    const mbcg_params p = r.p;
+    r.fetching += 1; // release waits until this copy is done
+    lk.unlock();
+    const size_t row = static_cast<size_t>(p.nx) * sizeof(float);
+    const size_t rows = static_cast<size_t>(p.ny) * p.nz;
+    cudaError_t e = cudaSuccess;
+    if (p.precision == MBCG_FP32) {
+        for (int i = 0; i < NF && e == cudaSuccess; ++i)
+            e = cudaMemcpy2DAsync(host[i], row, P.a[i], P.pitch * sizeof(float), row, rows, cudaMemcpyDeviceToHost,
+                                  s->st_io);
+    } else {
+        float* staging = nullptr;
+        const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
+        e = cudaMalloc(&staging, n * sizeof(float));
+        for (int i = 0; i < NF && e == cudaSuccess; ++i) {
+            e = launch_to_dense(p.precision, P, i, nullptr, staging, s->st_io);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(host[i], staging, n * sizeof(float), cudaMemcpyDeviceToHost, s->st_io);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->st_io);
+        }
+        if (staging) cudaFree(staging);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st_io);
+    lk.lock();
+    r.fetching -= 1;
+    s->cv_done.notify_all();
+    if (e != cudaSuccess) return cuda_fail(e, "mbcg_server_fetch");
+    return MBCG_OK;
+}
+
+int mbcg_server_release(mbcg_server* s, int64_t id) {
+    if (!s) return fail(MBCG_E_INVALID, "null server");
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(id);
+        if (it == s->reqs.end()) return fail(MBCG_E_INVALID, "unknown request id");
+        Request& r = *it->second;
+        if (r.state != MBCG_REQ_DONE && r.state != MBCG_REQ_FAILED)
+            return fail(MBCG_E_INVALID, "request still queued or running");
+        while (r.fetching > 0) s->cv_done.wait(lk);
+        if (r.resident) {
+            s->arena.release(r.off, r.bytes);
+            r.resident = false;
+        }
+    }
+    s->cv_work.notify_all();
+    return MBCG_OK;
+}
+
+int mbcg_server_get_stats(mbcg_server* s, mbcg_server_stats* out) {
+    if (!s || !out) return fail(MBCG_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->failed = s->failed;
+    out->live = live_count(s);
+    out->queued = static_cast<int64_t>(s->pending.size());
+    out->node_updates = s->node_updates;
+    out->compositions = s->compositions;
+    out->replays = s->replays;
+    out->arena_bytes = static_cast<int64_t>(s->arena.size());
+    out->arena_peak_bytes = static_cast<int64_t>(s->arena.peak());
+    out->zchunk = s->last_z;
+    for (int k = 0; k < BK_COUNT; ++k) out->plane_ns[k] = s->plane_ns[k];
+    out->tile_overhead_planes = s->tile_ovh;
+    out->busy_s = (s->first_admit >= 0 && s->last_done >= 0) ? s->last_done - s->first_admit : 0.0;
+    return MBCG_OK;
+}
+
+} // extern "C"

@@ -238,6 +238,48 @@ class Diag(ctypes.Structure):
                 "nonfinite": self.nonfinite, "nodes": self.nodes}
 
 
+class ServerConfig(ctypes.Structure):
+    """Mirror of ``mbcg_server_config``."""
+    _fields_ = [("arena_bytes", ctypes.c_int64), ("max_live", ctypes.c_int32), ("chunk_steps", ctypes.c_int32),
+                ("keep_results", ctypes.c_int32), ("backfill", ctypes.c_int32), ("zchunk", ctypes.c_int32),
+                ("calibrate", ctypes.c_int32), ("policy", ctypes.c_int32), ("fill_waves", ctypes.c_int32)]
+
+
+POLICY_FIFO, POLICY_SJF = 0, 1
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+class RequestInfo(ctypes.Structure):
+    """Mirror of ``mbcg_request_info``."""
+    _fields_ = [("id", ctypes.c_int64), ("state", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("steps", ctypes.c_int64), ("steps_done", ctypes.c_int64), ("t_submit", ctypes.c_double),
+                ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double), ("state_hash", ctypes.c_uint64),
+                ("diag", Diag)]
+
+    def as_dict(self) -> dict:
+        return {"id": self.id, "state": self.state, "status": self.status, "steps": self.steps,
+                "steps_done": self.steps_done, "t_submit": self.t_submit, "t_admit": self.t_admit,
+                "t_done": self.t_done, "state_hash": self.state_hash, "diag": self.diag.as_dict()}
+
+
+class ServerStats(ctypes.Structure):
+    """Mirror of ``mbcg_server_stats``."""
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("live", ctypes.c_int64), ("queued", ctypes.c_int64), ("node_updates", ctypes.c_int64),
+                ("compositions", ctypes.c_int64), ("replays", ctypes.c_int64), ("arena_bytes", ctypes.c_int64),
+                ("arena_peak_bytes", ctypes.c_int64), ("zchunk", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("plane_ns", ctypes.c_double * 10), ("tile_overhead_planes", ctypes.c_double),
+                ("busy_s", ctypes.c_double)]
+
+    BODIES = ("q19_f32", "q19_f16", "q19_bf16", "q27_f32", "q27_f16", "q27_bf16",
+              "q19_f32_periodic", "q19_f16_periodic", "q27_f32_periodic", "q27_f16_periodic")
+
+    def as_dict(self) -> dict:
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n not in ("plane_ns", "reserved")}
+        d["plane_ns"] = dict(zip(self.BODIES, list(self.plane_ns)))
+        return d
+
+
 class MbcgError(RuntimeError):
     pass
 
@@ -269,6 +311,16 @@ _PROTOS = {
     "mbcg_active_nodes": (ctypes.c_int64, [_P(Params)]),
     "mbcg_diagnostics_static": (ctypes.c_int, [_P(Params), _P(Moments), _P(Diag), _VP]),
     "mbcg_launches_per_step": (ctypes.c_int32, [_VP]),
+    "mbcg_server_config_default": (None, [_P(ServerConfig)]),
+    "mbcg_server_create": (ctypes.c_int, [_P(ServerConfig), _P(_VP)]),
+    "mbcg_server_destroy": (ctypes.c_int, [_VP]),
+    "mbcg_server_submit": (ctypes.c_int, [_VP, _P(Params), ctypes.c_int64, _P(ctypes.c_int64)]),
+    "mbcg_server_poll": (ctypes.c_int, [_VP, ctypes.c_int64, _P(RequestInfo)]),
+    "mbcg_server_wait": (ctypes.c_int, [_VP, ctypes.c_int64, ctypes.c_double, _P(RequestInfo)]),
+    "mbcg_server_drain": (ctypes.c_int, [_VP, ctypes.c_double]),
+    "mbcg_server_fetch": (ctypes.c_int, [_VP, ctypes.c_int64, _VP * NFIELDS]),
+    "mbcg_server_release": (ctypes.c_int, [_VP, ctypes.c_int64]),
+    "mbcg_server_get_stats": (ctypes.c_int, [_VP, _P(ServerStats)]),
     "mbcg_last_error": (ctypes.c_char_p, []),
     "mbcg_version": (ctypes.c_char_p, []),
 }
@@ -407,6 +459,80 @@ class Case:
         self.lib.check(self.lib.mbcg_autotune(self.handle, int(repeats), ctypes.byref(ms), _stream_ptr(stream)),
                        "mbcg_autotune")
         return float(ms.value)
+
+
+def server_config(**kw) -> ServerConfig:
+    """mbcg_server_config with the library defaults, then the given fields."""
+    cfg = ServerConfig()
+    Library.get().mbcg_server_config_default(ctypes.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Server:
+    """Continuous-batching server (mbcg_server*): many cases resident on one GPU, advanced
+    together by the persistent batch kernel."""
+
+    def __init__(self, config: Optional[ServerConfig] = None, lib: Optional[Library] = None, **kw):
+        self.lib = lib or Library.get()
+        cfg = config if config is not None else server_config(**kw)
+        h = ctypes.c_void_p()
+        self.lib.check(self.lib.mbcg_server_create(ctypes.byref(cfg), ctypes.byref(h)), "mbcg_server_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mbcg_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, params: Params, nsteps: int) -> int:
+        rid = ctypes.c_int64(0)
+        p = params.copy()
+        self.lib.check(self.lib.mbcg_server_submit(self.handle, ctypes.byref(p), int(nsteps), ctypes.byref(rid)),
+                       "mbcg_server_submit")
+        return int(rid.value)
+
+    def poll(self, rid: int) -> RequestInfo:
+        info = RequestInfo()
+        self.lib.check(self.lib.mbcg_server_poll(self.handle, int(rid), ctypes.byref(info)), "mbcg_server_poll")
+        return info
+
+    def wait(self, rid: int, timeout: float = 600.0) -> RequestInfo:
+        info = RequestInfo()
+        self.lib.check(self.lib.mbcg_server_wait(self.handle, int(rid), float(timeout), ctypes.byref(info)),
+                       "mbcg_server_wait")
+        return info
+
+    def drain(self, timeout: float = 3600.0):
+        self.lib.check(self.lib.mbcg_server_drain(self.handle, float(timeout)), "mbcg_server_drain")
+
+    def fetch(self, rid: int, shape) -> np.ndarray:
+        """Final state of a finished request (keep_results) as (11, nz, ny, nx) float32."""
+        out = np.empty((NFIELDS,) + tuple(shape), dtype=np.float32)
+        ptrs = (_VP * NFIELDS)(*[out[f].ctypes.data for f in range(NFIELDS)])
+        self.lib.check(self.lib.mbcg_server_fetch(self.handle, int(rid), ptrs), "mbcg_server_fetch")
+        return out
+
+    def release(self, rid: int):
+        self.lib.check(self.lib.mbcg_server_release(self.handle, int(rid)), "mbcg_server_release")
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        self.lib.check(self.lib.mbcg_server_get_stats(self.handle, ctypes.byref(st)), "mbcg_server_get_stats")
+        return st
 
 
 def moments_from_tensors(tensors: Sequence, pitch: int, precision: int = FP32) -> Moments:
