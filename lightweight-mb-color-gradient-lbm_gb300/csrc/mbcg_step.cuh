@@ -81,7 +81,7 @@ struct Geo {
     static constexpr int tx = 2 * RBY * kRBX * (int)sizeof(S) + 9 * MY * kMX * (int)sizeof(S);
     static constexpr int psi_plane = RBY * kPSX;           // floats
     static constexpr int psi = 3 * psi_plane * 4;          // bytes
-    static constexpr int xbuf_floats = 3 * 2 * 4 * W * 32; // [class][slot][comp][row][lane]
+    static constexpr int xbuf_floats = 3 * 2 * 4 * W * 32; // float4 [class][slot][row][lane]
     static constexpr int xbuf = xbuf_floats * 4;
     static constexpr int off_bar = 0;
     static constexpr int off_stage = 128;
@@ -371,7 +371,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                                           long long step, unsigned char* smem, uint32_t& phase) {
     using G = Geo<S, W>;
     float* psi_ring = reinterpret_cast<float*>(smem + G::off_psi);
-    float* xbuf = reinterpret_cast<float*>(smem + G::off_xbuf);
+    float4* xbuf = reinterpret_cast<float4*>(smem + G::off_xbuf);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + G::off_bar);
 
     const int lane = threadIdx.x;
@@ -551,20 +551,20 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
 
     constexpr float w0 = Stencil<Q>::wk(0);
     constexpr float cs2 = 1.0f / 3.0f;
-    float* xb_self = xbuf + w * 32 + lane;
+    float4* xb_self = xbuf + w * 32 + lane; // (X0, X1, X2, XR) of one exported row
 
     for (int k = zd0 - 1; k <= zd1; ++k) {
-        // (1) psi of plane k+1
+        // (1) psi of plane k+1; one barrier both publishes the ring and makes the bail decision
+        // uniform (a plane that never arrived leaves garbage in the ring, which nobody reads)
         {
             const bool ok = wait_stage(k + 1);
+            if (ok) fill_psi(k + 1, true);
             if (__syncthreads_or(!ok)) {
                 bail(k, k_issued);
                 return false;
             }
         }
-        fill_psi(k + 1, true);
         if (k + 2 <= zd1 + 1) prefetch_psi(k + 2);
-        __syncthreads();
         // (2) prefetch plane k+2 into the slot plane k-1 used
         if (k + 2 <= zd1 + 1 && k + 2 > k_issued) {
             issue(k + 2);
@@ -846,18 +846,10 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 // cy = +1 goes to row w+1 (slot 0), cy = -1 to row w-1 (slot 1)
                 constexpr int cls = cz + 1;
                 if constexpr ((ROWS & 4) != 0) {
-                    float* b0 = xb_self + ((cls * 2 + 0) * 4) * (W * 32);
-                    b0[0 * W * 32] = X0[2];
-                    b0[1 * W * 32] = X1[2];
-                    b0[2 * W * 32] = X2[2];
-                    b0[3 * W * 32] = XR[2];
+                    xb_self[(cls * 2 + 0) * (W * 32)] = make_float4(X0[2], X1[2], X2[2], XR[2]);
                 }
                 if constexpr ((ROWS & 1) != 0) {
-                    float* b1 = xb_self + ((cls * 2 + 1) * 4) * (W * 32);
-                    b1[0 * W * 32] = X0[0];
-                    b1[1 * W * 32] = X1[0];
-                    b1[2 * W * 32] = X2[0];
-                    b1[3 * W * 32] = XR[0];
+                    xb_self[(cls * 2 + 1) * (W * 32)] = make_float4(X0[0], X1[0], X2[0], XR[0]);
                 }
             };
             do_class(std::integral_constant<int, -1>{}, accP);
@@ -874,10 +866,10 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             constexpr int cz = decltype(czc)::value;
             constexpr int cls = cz + 1;
             constexpr float f = (kSepW && cz == 0) ? 4.0f : 1.0f;
-            const float* p0 = xb_self - 32 + ((cls * 2 + 0) * 4) * (W * 32);
-            const float* m1 = xb_self + 32 + ((cls * 2 + 1) * 4) * (W * 32);
-            const float P0 = p0[0], P1 = p0[W * 32], P2 = p0[2 * W * 32], PR = p0[3 * W * 32];
-            const float M0 = m1[0], M1 = m1[W * 32], M2 = m1[2 * W * 32], MR = m1[3 * W * 32];
+            const float4 pv = xb_self[(cls * 2 + 0) * (W * 32) - 32]; // row w-1 exported cy = +1
+            const float4 mv = xb_self[(cls * 2 + 1) * (W * 32) + 32]; // row w+1 exported cy = -1
+            const float P0 = pv.x, P1 = pv.y, P2 = pv.z, PR = pv.w;
+            const float M0 = mv.x, M1 = mv.y, M2 = mv.z, MR = mv.w;
             const float s00 = P0 + M0;
             const float s10 = P1 + M1;
             const float d00 = P0 - M0;
