@@ -396,6 +396,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     const bool dest_thread = lane >= 1 && lane <= kTX && w >= 1 && w <= W - 2 && xs <= nx - 2 && ys <= ny - 2;
     const int rx = axis_role<kFeat>(P, 0, xs, nx);
     const int ry = axis_role<kFeat>(P, 1, ys, ny);
+    const bool in_xy = rx != R_OUT && ry != R_OUT;
     const int ia = P.inout_axis;
 
     // psi fill: each thread owns <= kPsiPer ring elements; their mapping never changes along z.
@@ -577,7 +578,10 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         if (rx == R_OUT || ry == R_OUT || rz == R_OUT) role = R_OUT;
         else if ((kFeat & F_WALL) && (rx == R_WALL || ry == R_WALL || rz == R_WALL)) role = R_WALL;
         else if ((kFeat & F_INOUT) && (rx == R_GHOST || ry == R_GHOST || rz == R_GHOST)) role = R_GHOST;
-        const bool active = (role == R_FLUID || role == R_GHOST);
+        // Sources outside the lattice (lanes / rows past the last ghost layer) only ever stream
+        // into nodes that are not destinations of this tile, so without walls every source is
+        // processed branch-free; wall ghost layers hold data and must not emit.
+        const bool active = ((kFeat & F_WALL) == 0) || (role == R_FLUID || role == R_GHOST);
 
         unsigned char* st = stage_ptr(k);
         Node<S> nd{};
@@ -628,6 +632,9 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             aR = nd.rb == 0.0f ? 1.0f : (nd.rr == 0.0f ? 0.0f : q1);
             if (!(kFeat & F_INOUT) || role == R_FLUID) {
                 iface = (4.0f * nd.rr * nd.rb * inv * inv) > 1.0e-4f; // lbm.cuh:181,187
+                // zero-filled staging outside the lattice decodes to a mixed node in the 16-bit
+                // forms; keep those (never written) sources off the interface path
+                if constexpr (sizeof(S) != 4) iface = iface && in_xy;
                 build_coef<kFeat>(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, nd.ux, nd.uy, nd.uz, nd.pxx, nd.pxy,
                                   nd.pyy, nd.pyz, nd.pzz, nd.pxz);
             } else {

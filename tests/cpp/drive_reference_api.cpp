@@ -1,6 +1,7 @@
 // A driver written against the reference's host API names (include/mbcg_lbm.hpp), following
 // the reference's main loop (main.cu:25-55): allocate, initialise the jet, then RCS, jet
-// boundary conditions and swap per step, with the MLUPS counter; prints per-field sums.
+// boundary conditions and swap per step, with the MLUPS counter; prints per-field sums and sums of
+// magnitudes.
 #include <cstdio>
 #include <vector>
 
@@ -28,15 +29,24 @@ int main(int argc, char** argv) {
     const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
     std::vector<float> h(n);
     real_t* f[MBCG_NFIELDS] = {d.A.rhor, d.A.rhob, d.A.ux, d.A.uy, d.A.uz, d.A.Pixx, d.A.Pixy, d.A.Piyy, d.A.Piyz, d.A.Pizz, d.A.Pixz};
-    std::printf("{\"steps\": %d, \"mlups\": %.3f, \"sums\": [", steps, mlups_value(mlups));
+    double sums[MBCG_NFIELDS], abs_sums[MBCG_NFIELDS];
     for (int i = 0; i < MBCG_NFIELDS; ++i) {
         cudaMemcpy(h.data(), f[i], n * sizeof(float), cudaMemcpyDeviceToHost);
-        double s = 0.0;
+        double s = 0.0, a = 0.0;
         for (int z = 1; z < p.nz - 1; ++z)
             for (int y = 0; y < p.ny; ++y)
-                for (int x = 1; x < p.nx - 1; ++x) s += h[x + p.nx * (y + static_cast<size_t>(p.ny) * z)];
-        std::printf("%s%.17g", i ? ", " : "", s);
+                for (int x = 1; x < p.nx - 1; ++x) {
+                    const double v = h[x + p.nx * (y + static_cast<size_t>(p.ny) * z)];
+                    s += v;
+                    a += v < 0 ? -v : v;
+                }
+        sums[i] = s;
+        abs_sums[i] = a;
     }
+    std::printf("{\"steps\": %d, \"mlups\": %.3f, \"sums\": [", steps, mlups_value(mlups));
+    for (int i = 0; i < MBCG_NFIELDS; ++i) std::printf("%s%.17g", i ? ", " : "", sums[i]);
+    std::printf("], \"abs_sums\": [");
+    for (int i = 0; i < MBCG_NFIELDS; ++i) std::printf("%s%.17g", i ? ", " : "", abs_sums[i]);
     std::printf("]}\n");
     mlups_destroy(mlups);
     free_device_memory(d);

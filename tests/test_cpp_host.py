@@ -39,5 +39,9 @@ def test_reference_api_driver_matches_case_api(tmp_path):
         s = c.copy_out().astype(np.float64)
     sums = [s[f, 1:-1, :, 1:-1].sum() for f in range(11)]
     assert out["mlups"] > 0
-    for a, b in zip(out["sums"], sums):
-        assert abs(a - b) <= 1e-6 * (abs(b) + 1e-3), (out["sums"], sums)
+    # The driver's split launches on the reference's dense layout run the plain-load kernel,
+    # the case API the TMA kernel: separate compilations that may fuse different multiply-add
+    # pairs, so per-field sums agree to FP32 round-off relative to the field's magnitude (sums
+    # of the velocity fields cancel to ~1e-7 and carry no relative precision of their own).
+    for a, b, m in zip(out["sums"], sums, out["abs_sums"]):
+        assert abs(a - b) <= 1e-5 * m + 1e-12, (out["sums"], sums)

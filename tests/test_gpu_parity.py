@@ -137,9 +137,11 @@ def test_wall_axis_generality(axis):
 
 
 def test_tma_and_plain_load_paths_agree():
+    """Staging by TMA or by plain loads feeds the same arithmetic (both kernels carrying every
+    feature, as the plain-load path always does): bit-identical fields."""
     p = mbcg.jet_params(40, 36, 30, q=27, diameter=10.0)
     a = ol.oracle_init(p, np.float64)
-    t = gpu_run(p, a, 30)
+    t = gpu_run(p, a, 30, env={"MBCG_ALL_FEATURES": "1"})
     s = gpu_run(p, a, 30, env={"MBCG_NO_TMA": "1"})
     np.testing.assert_array_equal(t, s)
 

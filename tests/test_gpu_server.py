@@ -3,14 +3,16 @@ match the single-case API; admission respects the arena; bookkeeping is exact.
 
 Tolerances: a lattice served alone or in any mix runs the same batch-kernel code on the same
 data, so its final state is compared bit for bit (fetched fields and the 64-bit state hash).
-Against the single-case API (a separately compiled kernel that may fuse different
-multiply-add pairs) the gate is the FP32 parity gate, relative L2 <= 1e-5 per moment group.
+The single-case API runs a separately compiled kernel (which may fuse different multiply-add
+pairs), so served and single-case results are each held to the parity gates against the FP64
+oracle instead.
 """
 import numpy as np
 import pytest
 
 import mbcg
-from gpu_util import group_errors, written_nodes
+import oracle_lib as ol
+from gpu_util import assert_fp32_parity, group_errors, written_nodes
 
 pytestmark = pytest.mark.gpu
 
@@ -62,18 +64,49 @@ def test_same_result_alone_and_in_the_mix():
             srv.release(rid)
 
 
-def test_server_matches_single_case_api():
+# 16-bit storage: colour densities by relative L2 (the storage-form bounds of the jet test);
+# velocity and stress by RMS error in units of their storage scale (u_ref, pi_scale), since a
+# static bubble's velocities are spurious currents far below the scale, where relative errors
+# measure only the format's resolution
+FORM_BOUNDS = {mbcg.FP16: {"rhor": 5e-3, "rhob": 1e-3, "u": 2e-3, "Pi": 2e-3},
+               mbcg.BF16: {"rhor": 5e-2, "rhob": 1e-2, "u": 2e-2, "Pi": 2e-2}}
+
+
+def form_errors(got, ref, idx, p):
+    e = group_errors(got, ref, idx)
+    g, r = got[idx], ref[idx]
+    e["u"] = float(np.sqrt(np.mean((g[2:5].astype(np.float64) - r[2:5]) ** 2))) / p.u_ref
+    e["Pi"] = float(np.sqrt(np.mean((g[5:11].astype(np.float64) - r[5:11]) ** 2))) / p.pi_scale
+    return e
+
+
+def test_server_and_single_case_api_match_the_oracle():
+    """FP32: served results and single-case results both meet the parity gate against the FP64
+    oracle run from the same initial condition (the FP32 gate: relative L2 1e-5, or 3x the
+    reference's own FP32 arithmetic where that is larger); in FP16 / BF16 storage the served
+    and single-case runs agree within FORM_BOUNDS."""
     cases = mix_cases()
     alone = run_alone(cases)
     for (p, n), (_, f, info) in zip(cases, alone):
         with mbcg.Case(p) as c:
             c.init()
             c.step(n)
-            ref = c.copy_out()
+            single = c.copy_out()
             d = c.diagnostics()
-        for k, e in group_errors(f, ref, written_nodes(p)).items():
-            assert e <= 1e-5, (p.describe(), k, e)
-        assert abs(info["diag"]["mass_r"] - d["mass_r"]) <= 1e-6 * abs(d["mass_r"]) + 1e-9
+        idx = written_nodes(p)
+        if p.precision == mbcg.FP32:
+            a0 = ol.oracle_init(p, np.float64)
+            ref64 = ol.oracle_run(p, a0.copy(), n)
+            ref32 = ol.oracle_run(p, a0.astype(np.float32), n)
+            assert_fp32_parity(f, ref64, ref32, idx, what=f"served {p.describe()['ic']}")
+            assert_fp32_parity(single, ref64, ref32, idx, what=f"single {p.describe()['ic']}")
+        else:
+            # the 16-bit forms' own accuracy is the subject of tests/test_gpu_forms.py; here the
+            # served and single-case runs of the same form must agree within its resolution
+            e = form_errors(f, single, idx, p)
+            for k, lim in FORM_BOUNDS[p.precision].items():
+                assert e[k] < lim, (p.describe(), k, e)
+        assert abs(info["diag"]["mass_r"] - d["mass_r"]) <= 1e-5 * abs(d["mass_r"]) + 1e-9
 
 
 def test_admission_by_footprint_and_accounting():
