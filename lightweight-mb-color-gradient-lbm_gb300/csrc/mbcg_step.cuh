@@ -426,8 +426,11 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         }
     }
 
-    auto slot_of = [&](int k) -> int { return (k - kfirst) % kNSTAGE; };
-    auto stage_ptr = [&](int k) -> unsigned char* { return smem + G::off_stage + slot_of(k) * G::stage; };
+    // Plane k lives in stage slot (k - kfirst) mod 3, and its psi in the ring slot of the same
+    // index; the z loop advances the slot incrementally.
+    auto nxt = [](int sl) -> int { return sl == kNSTAGE - 1 ? 0 : sl + 1; };
+    auto prv = [](int sl) -> int { return sl == 0 ? kNSTAGE - 1 : sl - 1; };
+    auto stage_at = [&](int sl) -> unsigned char* { return smem + G::off_stage + sl * G::stage; };
     auto rb_box = [&](unsigned char* st, int f) -> S* { return reinterpret_cast<S*>(st + f * G::rb_field); };
     auto m_box = [&](unsigned char* st, int f) -> S* {
         return reinterpret_cast<S*>(st + 2 * G::rb_field + (f - 2) * G::m_field);
@@ -435,12 +438,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     auto zload = [&](int k) -> int { return data_coord(P, 2, k, nz); };
 
     // ---- stage loader -------------------------------------------------------------
-    auto issue = [&](int k) {
-        unsigned char* st = stage_ptr(k);
+    auto issue = [&](int k, int sl) {
+        unsigned char* st = stage_at(sl);
         const int kz = zload(k);
         if constexpr (kTMA) {
             if (tid == 0) {
-                uint64_t* bar = &bars[slot_of(k)];
+                uint64_t* bar = &bars[sl];
                 fence_proxy_async();
                 mbar_expect_tx(bar, G::tx);
                 tma_load_3d(rb_box(st, 0), &maps[0], xr0, yb - 1, kz, bar);
@@ -470,25 +473,30 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         }
     };
     constexpr long long kWaitLimit = 4000000000LL; // ~2 s at 2 GHz
-    // parity of the j-th load of this tile: the slot's phase count before the tile plus j / 3
-    auto parity_of = [&](int j) -> uint32_t {
-        return static_cast<uint32_t>(((j / kNSTAGE) & 1) ^ ((phase >> (j % kNSTAGE)) & 1));
-    };
-    auto wait_stage = [&](int k) -> bool {
+    // Expected parity of the next phase of each slot's mbarrier; every completed wait flips it.
+    // It starts from the parities the previous tile of this CTA left.
+    uint32_t par = phase;
+    int k_waited = kfirst - 1; // last plane whose load was waited for
+    auto wait_slot = [&](int k, int sl) -> bool {
         if constexpr (kTMA) {
-            const int j = k - kfirst;
-            return mbar_wait_bounded(&bars[j % kNSTAGE], parity_of(j), kWaitLimit);
+            const bool ok = mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit);
+            if (ok) {
+                par ^= 1u << sl;
+                k_waited = k;
+            }
+            return ok;
         } else {
+            k_waited = k;
             return true;
         }
     };
     // on a failed wait: flag it, drain the copies still in flight (bounded) and leave
-    auto bail = [&](int k_failed, int k_issued) {
+    auto bail = [&](int k_issued) {
         if (tid == 0 && P.status) atomicOr(P.status, 1);
         if constexpr (kTMA) {
-            for (int k = k_failed + 1; k <= k_issued; ++k) {
-                const int j = k - kfirst;
-                mbar_wait_bounded(&bars[j % kNSTAGE], parity_of(j), kWaitLimit / 4);
+            for (int k = k_waited + 1; k <= k_issued; ++k) {
+                const int sl = (k - kfirst) % kNSTAGE;
+                mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit / 4);
             }
         }
     };
@@ -504,12 +512,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 pf1[j] = Codec<S>::to_f(static_cast<const S*>(P.a[1])[zo + psi_g[j]]);
             }
     };
-    auto fill_psi = [&](int k, bool prefetched) {
-        float* ring = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
+    auto fill_psi = [&](int k, int sl, bool prefetched) {
+        float* ring = psi_ring + sl * G::psi_plane;
         const int mz = psi_coord(P, 2, k, nz);
         const bool plane_in_box = (mz == zload(k));
         const long long zo = static_cast<long long>(mz) * P.plane;
-        unsigned char* st = stage_ptr(k);
+        unsigned char* st = stage_at(sl);
         const S* r0b = rb_box(st, 0);
         const S* r1b = rb_box(st, 1);
 #pragma unroll
@@ -532,17 +540,17 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     // every thread is done with the previous tile's shared memory before it is refilled
     __syncthreads();
     int k_issued = kfirst + kNSTAGE - 1;
-    for (int k = kfirst; k <= k_issued; ++k) issue(k);
+    for (int k = kfirst; k <= k_issued; ++k) issue(k, k - kfirst);
     if constexpr (!kTMA) __syncthreads();
     {
-        const bool ok = wait_stage(kfirst) && wait_stage(kfirst + 1);
+        const bool ok = wait_slot(kfirst, 0) && wait_slot(kfirst + 1, 1);
         if (__syncthreads_or(!ok)) {
-            bail(kfirst - 1, k_issued);
+            bail(k_issued);
             return false;
         }
     }
-    fill_psi(kfirst, false);
-    fill_psi(kfirst + 1, false);
+    fill_psi(kfirst, 0, false);
+    fill_psi(kfirst + 1, 1, false);
     prefetch_psi(kfirst + 2);
 
     Acc accP, accC, accN; // destination planes k-1, k, k+1
@@ -554,21 +562,23 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     constexpr float cs2 = 1.0f / 3.0f;
     float4* xb_self = xbuf + w * 32 + lane; // (X0, X1, X2, XR) of one exported row
 
-    for (int k = zd0 - 1; k <= zd1; ++k) {
+    int sl = 1; // slot of plane k (k starts at kfirst + 1)
+    for (int k = zd0 - 1; k <= zd1; ++k, sl = nxt(sl)) {
+        const int sl_next = nxt(sl), sl_prev = prv(sl);
         // (1) psi of plane k+1; one barrier both publishes the ring and makes the bail decision
         // uniform (a plane that never arrived leaves garbage in the ring, which nobody reads)
         {
-            const bool ok = wait_stage(k + 1);
-            if (ok) fill_psi(k + 1, true);
+            const bool ok = wait_slot(k + 1, sl_next);
+            if (ok) fill_psi(k + 1, sl_next, true);
             if (__syncthreads_or(!ok)) {
-                bail(k, k_issued);
+                bail(k_issued);
                 return false;
             }
         }
         if (k + 2 <= zd1 + 1) prefetch_psi(k + 2);
         // (2) prefetch plane k+2 into the slot plane k-1 used
         if (k + 2 <= zd1 + 1 && k + 2 > k_issued) {
-            issue(k + 2);
+            issue(k + 2, sl_prev);
             k_issued = k + 2;
         }
 
@@ -583,7 +593,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         // processed branch-free; wall ghost layers hold data and must not emit.
         const bool active = ((kFeat & F_WALL) == 0) || (role == R_FLUID || role == R_GHOST);
 
-        unsigned char* st = stage_ptr(k);
+        unsigned char* st = stage_at(sl);
         Node<S> nd{};
         Node<S> fn{}; // first-fluid node of a ghost source (lbm.cuh:85-89)
         if (active) {
@@ -601,7 +611,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                     const unsigned char* sf = st;
                     int b2 = bM;
                     if (rz == R_GHOST) {
-                        sf = stage_ptr(k == 0 ? k + 1 : k - 1);
+                        sf = stage_at(k == 0 ? sl_next : sl_prev);
                     } else {
                         const int dx = (rx == R_GHOST) ? (xs == 0 ? 1 : -1) : 0;
                         const int dy = (ry == R_GHOST) ? (ys == 0 ? 1 : -1) : 0;
@@ -645,9 +655,9 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         const bool any_iface = __any_sync(kFull, iface);
         if (any_iface && iface) {
             // colour gradient at the source (forces.cuh:20-60) from the psi ring
-            const float* rm = psi_ring + ((k - 1 - kfirst) % 3) * G::psi_plane;
-            const float* r0p = psi_ring + ((k - kfirst) % 3) * G::psi_plane;
-            const float* rp = psi_ring + ((k + 1 - kfirst) % 3) * G::psi_plane;
+            const float* rm = psi_ring + sl_prev * G::psi_plane;
+            const float* r0p = psi_ring + sl * G::psi_plane;
+            const float* rp = psi_ring + sl_next * G::psi_plane;
             float sx = 0.0f, sy = 0.0f, sz = 0.0f;
 #pragma unroll
             for (int dz = -1; dz <= 1; ++dz) {
@@ -1021,15 +1031,8 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         accC = accN;
         accN.zero();
     }
-    // every load of this tile completed one phase of its slot: carry the parities over
-    if constexpr (kTMA) {
-        const int jlast = k_issued - kfirst;
-#pragma unroll
-        for (int sl = 0; sl < kNSTAGE; ++sl) {
-            const int loads = sl <= jlast ? (jlast - sl) / kNSTAGE + 1 : 0;
-            if (loads & 1) phase ^= 1u << sl;
-        }
-    }
+    // every load of this tile was waited for: carry the parities over to the next tile
+    phase = par;
     return true;
 }
 
