@@ -11,7 +11,8 @@
  * State: 11 SoA moment fields per node, in this order (memory.cuh:14-29):
  *   0 rhor, 1 rhob, 2 ux, 3 uy, 4 uz, 5 Pixx, 6 Pixy, 7 Piyy, 8 Piyz, 9 Pizz, 10 Pixz.
  * In the FP16/BF16 storage form the same 11 slots hold scaled deviations:
- *   0 (rho - rho_nominal(phi)) / rho_scale, 1 phi = (rhor-rhob)/rho,
+ *   0 (rho - rho_nominal(phi)) / rho_scale, 1 the colour complement
+ *   c = sign(phi) (1 - |phi|) of phi = (rhor-rhob)/rho (+0 pure red, -0 pure blue),
  *   2..4 u / u_ref, 5..10 Pi / pi_scale.
  *
  * Every function returns 0 on success and a negative MBCG_E* code on failure; the text of

@@ -21,10 +21,9 @@ __device__ __forceinline__ void load_node(const StepParams& P, const void* const
 template <typename S>
 __device__ __forceinline__ void to_moments(const StepParams& P, float (&v)[NF]) {
     if constexpr (sizeof(S) != 4) {
-        const float phi = v[1];
+        const float phi = phi_of_slot(v[1]);
         const float rho = P.rho_mean + phi * P.rho_half_diff + P.rho_scale * v[0];
-        v[0] = 0.5f * rho * (1.0f + phi);
-        v[1] = 0.5f * rho * (1.0f - phi);
+        colour_split(v[1], rho, v[0], v[1]);
         for (int i = 2; i < 5; ++i) v[i] *= P.u_ref;
         for (int i = 5; i < NF; ++i) v[i] *= P.pi_scale;
     }
@@ -38,9 +37,10 @@ __device__ __forceinline__ void store_moments(const StepParams& P, void* const* 
         for (int i = 0; i < NF; ++i) static_cast<float*>(f[i])[o] = m[i];
     } else {
         const float rho = m[0] + m[1];
-        const float phi = (m[0] - m[1]) / rho;
+        const S c = Codec<S>::from_f(colour_slot(m[0], m[1], rho));
+        const float phi = phi_of_slot(Codec<S>::to_f(c)); // the phi a reader decodes
         static_cast<S*>(f[0])[o] = Codec<S>::from_f((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale);
-        static_cast<S*>(f[1])[o] = Codec<S>::from_f(phi);
+        static_cast<S*>(f[1])[o] = c;
         for (int i = 2; i < 5; ++i) static_cast<S*>(f[i])[o] = Codec<S>::from_f(m[i] * P.inv_u_ref);
         for (int i = 5; i < NF; ++i) static_cast<S*>(f[i])[o] = Codec<S>::from_f(m[i] * P.inv_pi_scale);
     }
@@ -342,9 +342,11 @@ __global__ void to_dense_kernel(const StepParams P, int field, float* dst) {
         } else {
             if (field <= 1) {
                 const float s0 = Codec<S>::to_f(static_cast<const S*>(P.a[0])[o]);
-                const float phi = Codec<S>::to_f(static_cast<const S*>(P.a[1])[o]);
-                const float rho = P.rho_mean + phi * P.rho_half_diff + P.rho_scale * s0;
-                v = field == 0 ? 0.5f * rho * (1.0f + phi) : 0.5f * rho * (1.0f - phi);
+                const float c = Codec<S>::to_f(static_cast<const S*>(P.a[1])[o]);
+                const float rho = P.rho_mean + phi_of_slot(c) * P.rho_half_diff + P.rho_scale * s0;
+                float rr, rb;
+                colour_split(c, rho, rr, rb);
+                v = field == 0 ? rr : rb;
             } else {
                 const float s = Codec<S>::to_f(static_cast<const S*>(P.a[field])[o]);
                 v = s * (field < 5 ? P.u_ref : P.pi_scale);

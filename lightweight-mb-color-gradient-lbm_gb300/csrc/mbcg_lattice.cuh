@@ -69,8 +69,9 @@ enum Field : int { RHOR = 0, RHOB, UX, UY, UZ, PXX, PXY, PYY, PYZ, PZZ, PXZ, NF 
 
 // ------------------------------------------------------------------ storage codecs
 // FP32 stores the reference's moments as they are.  FP16 / BF16 store scaled deviations:
-// slot 0 (rho - rho_nominal(phi)) / rho_scale, slot 1 phi, 2..4 u / u_ref, 5..10 Pi / pi_scale,
-// with rho_nominal(phi) = (rho_r0 + rho_b0)/2 + phi (rho_r0 - rho_b0)/2.
+// slot 0 (rho - rho_nominal(phi)) / rho_scale, slot 1 the colour complement c (colour_slot),
+// 2..4 u / u_ref, 5..10 Pi / pi_scale, with rho_nominal(phi) = (rho_r0 + rho_b0)/2 +
+// phi (rho_r0 - rho_b0)/2 evaluated at the stored (rounded) phi.
 template <typename S>
 struct Codec;
 
@@ -92,6 +93,30 @@ struct Codec<__nv_bfloat16> {
     static __device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
     static __device__ __forceinline__ __nv_bfloat16 from_f(float v) { return __float2bfloat16_rn(v); }
 };
+
+// Colour slot of the 16-bit forms.  It holds the complement of the colour field,
+// c = sign(phi) (1 - |phi|) = +2 rho_b / rho (phi >= 0) or -2 rho_r / rho (phi < 0), not phi
+// itself: near the pure phases phi rounds to +-1 in 16 bits (resolution 2^-11) and the minority
+// colour would vanish, while c keeps its full relative precision there.  Pure red is c = +0,
+// pure blue c = -0.
+MBCG_HD float colour_slot(float rr, float rb, float rho) {
+#ifdef __CUDA_ARCH__
+    // a 2-ulp quotient is ample for a 16-bit slot
+    return rr >= rb ? __fdividef(2.0f * rb, rho) : -__fdividef(2.0f * rr, rho);
+#else
+    return rr >= rb ? 2.0f * rb / rho : -(2.0f * rr / rho);
+#endif
+}
+MBCG_HD float phi_of_slot(float c) { return copysignf(1.0f - fabsf(c), c); }
+// colour densities from rho and the slot: the minority colour is rho |c| / 2 directly (forming
+// 1 + phi in FP32 would cancel away the digits c keeps), the majority the rest
+MBCG_HD void colour_split(float c, float rho, float& rr, float& rb) {
+    const float minor = 0.5f * rho * fabsf(c);
+    const float major = rho - minor;
+    const bool red_major = !signbit(c);
+    rr = red_major ? major : minor;
+    rb = red_major ? minor : major;
+}
 
 // ------------------------------------------------------------------ parameter block
 struct StepParams {

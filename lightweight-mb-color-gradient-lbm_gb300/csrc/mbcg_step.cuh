@@ -169,7 +169,7 @@ __device__ __forceinline__ float psi_of(const StepParams& P, S s0, S s1) {
     } else {
         (void)P;
         (void)s0;
-        return Codec<S>::to_f(s1);
+        return phi_of_slot(Codec<S>::to_f(s1));
     }
 }
 
@@ -177,7 +177,7 @@ __device__ __forceinline__ float psi_of(const StepParams& P, S s0, S s1) {
 template <typename S>
 __device__ __forceinline__ float psi_of_slots(float v0, float v1) {
     if constexpr (std::is_same<S, float>::value) return __fdividef(v0 - v1, v0 + v1);
-    else return v1;
+    else return phi_of_slot(v1);
 }
 
 // decode the 11 stored slots into the reference's moments
@@ -187,10 +187,9 @@ __device__ __forceinline__ void decode(const StepParams& P, const float (&v)[NF]
         n.rr = v[0]; n.rb = v[1]; n.ux = v[2]; n.uy = v[3]; n.uz = v[4];
         n.pxx = v[5]; n.pxy = v[6]; n.pyy = v[7]; n.pyz = v[8]; n.pzz = v[9]; n.pxz = v[10];
     } else {
-        const float phi = v[1];
+        const float phi = phi_of_slot(v[1]);
         const float rho = P.rho_mean + phi * P.rho_half_diff + P.rho_scale * v[0];
-        n.rr = 0.5f * rho * (1.0f + phi);
-        n.rb = 0.5f * rho * (1.0f - phi);
+        colour_split(v[1], rho, n.rr, n.rb);
         n.ux = P.u_ref * v[2]; n.uy = P.u_ref * v[3]; n.uz = P.u_ref * v[4];
         n.pxx = P.pi_scale * v[5]; n.pxy = P.pi_scale * v[6]; n.pyy = P.pi_scale * v[7];
         n.pyz = P.pi_scale * v[8]; n.pzz = P.pi_scale * v[9]; n.pxz = P.pi_scale * v[10];
@@ -205,9 +204,9 @@ __device__ __forceinline__ void encode(const StepParams& P, float rr, float rb, 
         for (int i = 0; i < 6; ++i) out[5 + i] = pi[i];
     } else {
         const float rho = rr + rb;
-        const float phi = (rr - rb) / rho;
+        out[1] = Codec<S>::from_f(colour_slot(rr, rb, rho));
+        const float phi = phi_of_slot(Codec<S>::to_f(out[1])); // the phi a reader decodes
         out[0] = Codec<S>::from_f((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale);
-        out[1] = Codec<S>::from_f(phi);
         for (int i = 0; i < 3; ++i) out[2 + i] = Codec<S>::from_f(u[i] * P.inv_u_ref);
         for (int i = 0; i < 6; ++i) out[5 + i] = Codec<S>::from_f(pi[i] * P.inv_pi_scale);
     }

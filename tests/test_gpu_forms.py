@@ -34,10 +34,13 @@ def test_fp32_form_vs_fp64(oracle_states):
 
 
 # FP16 / BF16 bounds: what the scaled-deviation forms reach at 100 steps (relative L2 against
-# the FP64 oracle, per colour density, velocity field and stress field); the FP16 target of
-# 1e-3 for every field is not met yet for rhor and Pi (see the printed errors)
-@pytest.mark.parametrize("prec,tol100", [(mbcg.FP16, {"rhor": 5e-3, "rhob": 1e-3, "u": 1e-3, "Pi": 5e-3}),
-                                         (mbcg.BF16, {"rhor": 5e-2, "rhob": 1e-2, "u": 1e-2, "Pi": 5e-2})])
+# the FP64 oracle, per colour density, velocity field and stress field; measured FP16 1.0e-4,
+# 6.7e-6, 4.6e-4, 2.6e-3 and BF16 1.3e-3, 8.2e-5, 3.7e-3, 2.1e-2).  The FP16 target of 1e-3 holds
+# for the densities and the velocity; the stress field misses it: 16-bit velocity resolution
+# alone puts 2.4e-3 into Pi (Pi is ~25x smaller than rho u u, which carries the rounding), as
+# an FP64 run that rounds only the stored velocity to FP16 after every step reproduces.
+@pytest.mark.parametrize("prec,tol100", [(mbcg.FP16, {"rhor": 5e-4, "rhob": 5e-5, "u": 1e-3, "Pi": 5e-3}),
+                                         (mbcg.BF16, {"rhor": 5e-3, "rhob": 5e-4, "u": 1e-2, "Pi": 5e-2})])
 def test_storage_form_error_vs_fp64(oracle_states, prec, tol100):
     p32, a, s100, s1000, _ = oracle_states
     p = jet(prec)
