@@ -3,6 +3,8 @@
 // FP64 conservation / Laplace diagnostics and the dense-layout conversions used by
 // copy-in / copy-out.  None of these is on the per-step hot path of mbcg_step().
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <cstdint>
 
 #include "mbcg_internal.h"
@@ -327,20 +329,20 @@ __global__ void diag_final_kernel(const double* partials, int nparts, double* re
 }
 
 // ---------------------------------------------------------------- dense conversions
+// One field between the library layout (padded pitch, 16-bit slots) and the reference's dense
+// FP32 layout (pitch nx).  A block walks whole rows, so the index arithmetic is per row.
 template <typename S>
-__global__ void to_dense_kernel(const StepParams P, int field, float* dst) {
-    const long long total = static_cast<long long>(P.nx) * P.ny * P.nz;
-    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
-         e += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int x = static_cast<int>(e % P.nx);
-        const int y = static_cast<int>((e / P.nx) % P.ny);
-        const int z = static_cast<int>(e / (static_cast<long long>(P.nx) * P.ny));
-        const long long o = lin(P, x, y, z);
-        float v;
-        if constexpr (sizeof(S) == 4) {
-            v = static_cast<const float*>(P.a[field])[o];
-        } else {
-            if (field <= 1) {
+__global__ void to_dense_kernel(const StepParams P, int field, float* __restrict__ dst) {
+    const long long rows = static_cast<long long>(P.ny) * P.nz;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const long long o0 = (r / P.ny) * P.plane + (r % P.ny) * P.pitch;
+        float* d = dst + r * P.nx;
+        for (int x = threadIdx.x; x < P.nx; x += blockDim.x) {
+            const long long o = o0 + x;
+            float v;
+            if constexpr (sizeof(S) == 4) {
+                v = static_cast<const float*>(P.a[field])[o];
+            } else if (field <= 1) {
                 const float s0 = Codec<S>::to_f(static_cast<const S*>(P.a[0])[o]);
                 const float c = Codec<S>::to_f(static_cast<const S*>(P.a[1])[o]);
                 const float rho = P.rho_mean + phi_of_slot(c) * P.rho_half_diff + P.rho_scale * s0;
@@ -348,32 +350,49 @@ __global__ void to_dense_kernel(const StepParams P, int field, float* dst) {
                 colour_split(c, rho, rr, rb);
                 v = field == 0 ? rr : rb;
             } else {
-                const float s = Codec<S>::to_f(static_cast<const S*>(P.a[field])[o]);
-                v = s * (field < 5 ? P.u_ref : P.pi_scale);
+                v = Codec<S>::to_f(static_cast<const S*>(P.a[field])[o]) * (field < 5 ? P.u_ref : P.pi_scale);
             }
+            d[x] = v;
         }
-        dst[e] = v;
     }
 }
 
-// dense FP32 moments (all 11 fields, reference layout) -> stored slots
+// Dense FP32 field(s) -> the state P.b.  The 16-bit forms store rho and the colour slot from
+// rhor and rhob together: field 0 there takes src (rhor) and src_b (rhob) and field 1 is empty.
 template <typename S>
-__global__ void from_dense_kernel(const StepParams P, const float* src) {
-    const long long total = static_cast<long long>(P.nx) * P.ny * P.nz;
-    for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < total;
-         e += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int x = static_cast<int>(e % P.nx);
-        const int y = static_cast<int>((e / P.nx) % P.ny);
-        const int z = static_cast<int>(e / (static_cast<long long>(P.nx) * P.ny));
-        float m[NF];
-        for (int i = 0; i < NF; ++i) m[i] = src[i * total + e];
-        if (m[0] + m[1] == 0.0f) {
-            // unused ghost node with no fluid: store zeros rather than 0/0
-            for (int i = 0; i < NF; ++i) static_cast<S*>(P.b[i])[lin(P, x, y, z)] = Codec<S>::from_f(0.0f);
-            continue;
+__global__ void from_dense_kernel(const StepParams P, int field, const float* __restrict__ src,
+                                  const float* __restrict__ src_b) {
+    const long long rows = static_cast<long long>(P.ny) * P.nz;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const long long o0 = (r / P.ny) * P.plane + (r % P.ny) * P.pitch;
+        const float* a = src + r * P.nx;
+        for (int x = threadIdx.x; x < P.nx; x += blockDim.x) {
+            const long long o = o0 + x;
+            if constexpr (sizeof(S) == 4) {
+                static_cast<float*>(P.b[field])[o] = a[x];
+            } else if (field == 0) {
+                const float rr = a[x], rb = src_b[r * P.nx + x];
+                const float rho = rr + rb;
+                if (rho == 0.0f) {
+                    // unused ghost node with no fluid: zeros rather than 0/0
+                    static_cast<S*>(P.b[0])[o] = Codec<S>::from_f(0.0f);
+                    static_cast<S*>(P.b[1])[o] = Codec<S>::from_f(0.0f);
+                    continue;
+                }
+                const S c = Codec<S>::from_f(colour_slot(rr, rb, rho));
+                const float phi = phi_of_slot(Codec<S>::to_f(c)); // the phi a reader decodes
+                static_cast<S*>(P.b[0])[o] = Codec<S>::from_f((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale);
+                static_cast<S*>(P.b[1])[o] = c;
+            } else if (field >= 2) {
+                static_cast<S*>(P.b[field])[o] = Codec<S>::from_f(a[x] * (field < 5 ? P.inv_u_ref : P.inv_pi_scale));
+            }
         }
-        store_moments<S>(P, P.b, lin(P, x, y, z), m);
     }
+}
+
+int rows_grid(const StepParams& P) {
+    const long long rows = static_cast<long long>(P.ny) * P.nz;
+    return static_cast<int>(std::min<long long>(rows, 65535));
 }
 
 template <typename S>
@@ -510,27 +529,21 @@ cudaError_t launch_diag(int precision, const StepParams& P, const mbcg_params& p
     }
 }
 
-cudaError_t launch_to_dense(int precision, const StepParams& P, int field, const void* src, float* dst,
-                            cudaStream_t s) {
-    (void)src;
-    const long long n = static_cast<long long>(P.nx) * P.ny * P.nz;
+cudaError_t launch_to_dense(int precision, const StepParams& P, int field, float* dst, cudaStream_t s) {
     switch (precision) {
-    case MBCG_FP16: to_dense_kernel<__half><<<grid_for(n), 256, 0, s>>>(P, field, dst); break;
-    case MBCG_BF16: to_dense_kernel<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>(P, field, dst); break;
-    default: to_dense_kernel<float><<<grid_for(n), 256, 0, s>>>(P, field, dst); break;
+    case MBCG_FP16: to_dense_kernel<__half><<<rows_grid(P), 256, 0, s>>>(P, field, dst); break;
+    case MBCG_BF16: to_dense_kernel<__nv_bfloat16><<<rows_grid(P), 256, 0, s>>>(P, field, dst); break;
+    default: to_dense_kernel<float><<<rows_grid(P), 256, 0, s>>>(P, field, dst); break;
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_from_dense(int precision, const StepParams& P, int field, const float* src, void* dst,
+cudaError_t launch_from_dense(int precision, const StepParams& P, int field, const float* src, const float* src_b,
                               cudaStream_t s) {
-    (void)field;
-    (void)dst;
-    const long long n = static_cast<long long>(P.nx) * P.ny * P.nz;
     switch (precision) {
-    case MBCG_FP16: from_dense_kernel<__half><<<grid_for(n), 256, 0, s>>>(P, src); break;
-    case MBCG_BF16: from_dense_kernel<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>(P, src); break;
-    default: from_dense_kernel<float><<<grid_for(n), 256, 0, s>>>(P, src); break;
+    case MBCG_FP16: from_dense_kernel<__half><<<rows_grid(P), 256, 0, s>>>(P, field, src, src_b); break;
+    case MBCG_BF16: from_dense_kernel<__nv_bfloat16><<<rows_grid(P), 256, 0, s>>>(P, field, src, src_b); break;
+    default: from_dense_kernel<float><<<rows_grid(P), 256, 0, s>>>(P, field, src, src_b); break;
     }
     return cudaGetLastError();
 }

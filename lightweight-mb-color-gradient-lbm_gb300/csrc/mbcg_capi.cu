@@ -250,6 +250,7 @@ struct mbcg_case {
     long long steps = 0;
     int w = kStepW;   // step CTA rows
     int zchunk = 16;  // destination planes per step CTA
+    float* stage = nullptr; // two dense FP32 fields for host copies, allocated on first use
 };
 
 namespace {
@@ -276,6 +277,7 @@ void free_case(mbcg_case* c) {
     if (c->status) cudaFree(c->status);
     if (c->diag_partials) cudaFree(c->diag_partials);
     if (c->diag_result) cudaFree(c->diag_result);
+    if (c->stage) cudaFree(c->stage);
     delete c;
 }
 
@@ -481,32 +483,20 @@ int mbcg_fields(const mbcg_case* c, mbcg_moments* a, mbcg_moments* b) {
 
 int64_t mbcg_steps_done(const mbcg_case* c) { return c ? c->steps : -1; }
 
+// Host copies move one whole dense field per transfer (one contiguous copy at full link
+// bandwidth: the reference's dense rows of nx floats would otherwise be copied row by row as a
+// pitched 2-D transfer) through a pair of dense device fields, converted on the device.
 int mbcg_copy_out(mbcg_case* c, float* const host[MBCG_NFIELDS], mbcg_stream_t s) {
     if (!c || !host) return fail(MBCG_E_INVALID, "null argument");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
     const mbcg_params& p = c->p;
-    const size_t row = static_cast<size_t>(p.nx) * sizeof(float);
-    const size_t rows = static_cast<size_t>(p.ny) * p.nz;
-    if (p.precision == MBCG_FP32) {
-        for (int i = 0; i < NF; ++i)
-            MBCG_TRY(cudaMemcpy2DAsync(host[i], row, c->fields[c->cur][i], c->pitch * sizeof(float), row, rows,
-                                       cudaMemcpyDeviceToHost, st),
-                     "copy out");
-    } else {
-        float* staging = nullptr;
-        const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
-        MBCG_TRY(cudaMalloc(&staging, n * sizeof(float)), "staging allocation");
-        StepParams P = make_params(c, c->cur, c->steps);
-        for (int i = 0; i < NF; ++i) {
-            cudaError_t e = launch_to_dense(p.precision, P, i, nullptr, staging, st);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(host[i], staging, n * sizeof(float), cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (e != cudaSuccess) {
-                cudaFree(staging);
-                return cuda_fail(e, "copy out");
-            }
-        }
-        cudaFree(staging);
+    const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
+    if (!c->stage) MBCG_TRY(cudaMalloc(&c->stage, 2 * n * sizeof(float)), "staging allocation");
+    StepParams P = make_params(c, c->cur, c->steps); // P.a = current state
+    for (int i = 0; i < NF; ++i) {
+        float* buf = c->stage + (i & 1) * n; // reused two fields later, in stream order
+        MBCG_TRY(launch_to_dense(p.precision, P, i, buf, st), "copy out");
+        MBCG_TRY(cudaMemcpyAsync(host[i], buf, n * sizeof(float), cudaMemcpyDeviceToHost, st), "copy out");
     }
     MBCG_TRY(cudaStreamSynchronize(st), "copy out");
     return MBCG_OK;
@@ -516,30 +506,18 @@ int mbcg_copy_in(mbcg_case* c, const float* const host[MBCG_NFIELDS], mbcg_strea
     if (!c || !host) return fail(MBCG_E_INVALID, "null argument");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
     const mbcg_params& p = c->p;
-    const size_t row = static_cast<size_t>(p.nx) * sizeof(float);
-    const size_t rows = static_cast<size_t>(p.ny) * p.nz;
-    if (p.precision == MBCG_FP32) {
-        for (int i = 0; i < NF; ++i)
-            MBCG_TRY(cudaMemcpy2DAsync(c->fields[c->cur][i], c->pitch * sizeof(float), host[i], row, row, rows,
-                                       cudaMemcpyHostToDevice, st),
-                     "copy in");
-    } else {
-        float* staging = nullptr;
-        const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
-        MBCG_TRY(cudaMalloc(&staging, NF * n * sizeof(float)), "staging allocation");
-        cudaError_t e = cudaSuccess;
-        for (int i = 0; i < NF && e == cudaSuccess; ++i)
-            e = cudaMemcpyAsync(staging + i * n, host[i], n * sizeof(float), cudaMemcpyHostToDevice, st);
-        StepParams P = make_params(c, c->cur ^ 1, c->steps); // P.b = current state
-        if (e == cudaSuccess) e = launch_from_dense(p.precision, P, 0, staging, nullptr, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        cudaFree(staging);
-        if (e != cudaSuccess) return cuda_fail(e, "copy in");
+    const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
+    if (!c->stage) MBCG_TRY(cudaMalloc(&c->stage, 2 * n * sizeof(float)), "staging allocation");
+    StepParams P = make_params(c, c->cur ^ 1, c->steps); // P.b = current state
+    const bool pair = p.precision != MBCG_FP32; // rhor and rhob convert together
+    for (int i = 0; i < NF; ++i) {
+        float* buf = c->stage + (i & 1) * n;
+        MBCG_TRY(cudaMemcpyAsync(buf, host[i], n * sizeof(float), cudaMemcpyHostToDevice, st), "copy in");
+        if (pair && i == 0) continue; // converted with field 1
+        if (pair && i == 1) MBCG_TRY(launch_from_dense(p.precision, P, 0, c->stage, c->stage + n, st), "copy in");
+        else MBCG_TRY(launch_from_dense(p.precision, P, i, buf, nullptr, st), "copy in");
     }
-    {
-        StepParams P = make_params(c, c->cur ^ 1, c->steps); // P.b = current state
-        MBCG_TRY(launch_fill_ghosts(p.precision, P, st), "ghost images");
-    }
+    MBCG_TRY(launch_fill_ghosts(p.precision, P, st), "ghost images");
     MBCG_TRY(cudaStreamSynchronize(st), "copy in");
     return MBCG_OK;
 }

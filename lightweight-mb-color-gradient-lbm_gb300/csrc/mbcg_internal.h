@@ -42,9 +42,10 @@ cudaError_t launch_init(int precision, const StepParams& P, const mbcg_params& p
 cudaError_t launch_diag(int precision, const StepParams& P, const mbcg_params& p, double* partials, int nparts,
                         double* result, cudaStream_t s);
 int diag_partials_needed(const StepParams& P);
-cudaError_t launch_to_dense(int precision, const StepParams& P, int field, const void* src, float* dst,
-                            cudaStream_t s);
-cudaError_t launch_from_dense(int precision, const StepParams& P, int field, const float* src, void* dst,
+// one field between the state and the reference's dense FP32 layout (P.a -> dst; src -> P.b,
+// where the 16-bit forms take rhor and rhob together as field 0 and skip field 1)
+cudaError_t launch_to_dense(int precision, const StepParams& P, int field, float* dst, cudaStream_t s);
+cudaError_t launch_from_dense(int precision, const StepParams& P, int field, const float* src, const float* src_b,
                               cudaStream_t s);
 
 // sets the message mbcg_last_error() returns on the calling thread (mbcg_capi.cu)

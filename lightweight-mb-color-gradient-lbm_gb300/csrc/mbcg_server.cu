@@ -1045,25 +1045,17 @@ int mbcg_server_fetch(mbcg_server* s, int64_t id, float* const host[MBCG_NFIELDS
     const mbcg_params p = r.p;
     r.fetching += 1; // release waits until this copy is done
     lk.unlock();
-    const size_t row = static_cast<size_t>(p.nx) * sizeof(float);
-    const size_t rows = static_cast<size_t>(p.ny) * p.nz;
-    cudaError_t e = cudaSuccess;
-    if (p.precision == MBCG_FP32) {
-        for (int i = 0; i < NF && e == cudaSuccess; ++i)
-            e = cudaMemcpy2DAsync(host[i], row, P.a[i], P.pitch * sizeof(float), row, rows, cudaMemcpyDeviceToHost,
-                                  s->st_io);
-    } else {
-        float* staging = nullptr;
-        const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
-        e = cudaMalloc(&staging, n * sizeof(float));
-        for (int i = 0; i < NF && e == cudaSuccess; ++i) {
-            e = launch_to_dense(p.precision, P, i, nullptr, staging, s->st_io);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(host[i], staging, n * sizeof(float), cudaMemcpyDeviceToHost, s->st_io);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s->st_io);
-        }
-        if (staging) cudaFree(staging);
+    // one dense field per transfer through a dense device field (see mbcg_copy_out)
+    const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
+    float* staging = nullptr;
+    cudaError_t e = cudaMalloc(&staging, 2 * n * sizeof(float));
+    for (int i = 0; i < NF && e == cudaSuccess; ++i) {
+        float* buf = staging + (i & 1) * n;
+        e = launch_to_dense(p.precision, P, i, buf, s->st_io);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(host[i], buf, n * sizeof(float), cudaMemcpyDeviceToHost, s->st_io);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st_io);
+    if (staging) cudaFree(staging);
     lk.lock();
     r.fetching -= 1;
     s->cv_done.notify_all();
