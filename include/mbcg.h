@@ -169,6 +169,43 @@ int mbcg_diagnostics(mbcg_case *c, mbcg_diag *out, mbcg_stream_t s);
 /* Reads and clears the device status word (non-zero = a bounded wait gave up). */
 int mbcg_status(mbcg_case *c, int32_t *status);
 
+/* The parameters the case was created with. */
+int mbcg_case_params(const mbcg_case *c, mbcg_params *out);
+
+/* ---- output: VTI images (io/vtiWriter.cuh:60-164) and checkpoints ---------------------- */
+#define MBCG_VTI_ASCII 0   /* the reference's encoding: Float32 ASCII DataArrays, "%.8e " per value,
+                              one x row per line (io/vtiWriter.cuh:60-85)                      */
+#define MBCG_VTI_RAW   1   /* the same arrays as VTK appended raw binary (UInt64 size headers) */
+/* field_mask: bit f selects field f (0 rhor ... 10 Pixz, as reference FP32 moments); 0 selects
+ * the reference's five fields rhor, rhob, ux, uy, uz (io/vtiWriter.cuh:88-127). */
+#define MBCG_VTI_REFERENCE_FIELDS 0x1Fu
+
+/* Writes state A of the case over the full lattice (ghost frame included, as the reference
+ * does) to path.  Synchronous (write_vti_step_device, io/vtiWriter.cuh:151-164). */
+int mbcg_write_vti(mbcg_case *c, const char *path, uint32_t field_mask, int32_t format, mbcg_stream_t s);
+
+/* Asynchronous VTI output (no counterpart in the reference, which stops the run to write).
+ * mbcg_writer_snapshot enqueues on stream s a dense copy of state A into one of max_pending
+ * device snapshot buffers and returns: steps enqueued on s afterwards may run at once.  The
+ * device-to-host copy runs on the writer's own stream and the file is written by the writer's
+ * thread, both overlapping later steps.  When every buffer holds a snapshot not yet on disk,
+ * snapshot blocks until one is written.  Each snapshot buffer holds the selected fields in
+ * device memory and in pinned host memory. */
+typedef struct mbcg_writer mbcg_writer;
+int mbcg_writer_create(int32_t max_pending, mbcg_writer **out);
+int mbcg_writer_snapshot(mbcg_writer *w, mbcg_case *c, const char *path, uint32_t field_mask,
+                         int32_t format, mbcg_stream_t s);
+/* Waits until every snapshot is on disk; returns the first write error since the last flush. */
+int mbcg_writer_flush(mbcg_writer *w);
+int mbcg_writer_destroy(mbcg_writer *w); /* flushes first */
+
+/* Checkpoint (no counterpart in the reference): a binary file with the case parameters, the step
+ * count (the inlet-noise counter) and the 11 stored fields in their storage precision over the
+ * full lattice, with an FNV-1a checksum.  A case restored by mbcg_checkpoint_load continues bit
+ * for bit as the saved case would have.  save synchronises s. */
+int mbcg_checkpoint_save(mbcg_case *c, const char *path, mbcg_stream_t s);
+int mbcg_checkpoint_load(const char *path, mbcg_case **out);
+
 /* ---- launch shape (no counterpart in the reference, whose block is the compile-time
  * 32x4x2 of compile.sh:34-36) --------------------------------------------------------- */
 /* Step CTA shape: block_rows warps (8 or 16) of 32 lanes; zchunk destination planes per CTA

@@ -322,6 +322,25 @@ StepParams raw_params(const mbcg_params* p, const mbcg_moments* a, const mbcg_mo
 
 } // namespace
 
+// Copies the current state into the other one.  A step never writes the wall ghost layers (or
+// nodes outside every boundary rule), so after this both states agree there for good and the
+// full box read back does not depend on the parity of the step count.
+int mbcg::mirror_state(mbcg_case* c, cudaStream_t s) {
+    const size_t bytes = static_cast<size_t>(c->fstride) * NF * c->es;
+    MBCG_TRY(cudaMemcpyAsync(c->buf[c->cur ^ 1], c->buf[c->cur], bytes, cudaMemcpyDeviceToDevice, s), "state mirror");
+    return MBCG_OK;
+}
+
+int mbcg::case_field_to_dense(mbcg_case* c, int field, float* dst, cudaStream_t s) {
+    if (!c || !dst || field < 0 || field >= NF) return fail(MBCG_E_INVALID, "bad field snapshot request");
+    StepParams P = make_params(c, c->cur, c->steps); // P.a = current state
+    MBCG_TRY(launch_to_dense(c->p.precision, P, field, dst, s), "field snapshot");
+    return MBCG_OK;
+}
+void mbcg::case_set_steps(mbcg_case* c, long long steps) {
+    if (c) c->steps = steps;
+}
+
 extern "C" {
 
 void mbcg_params_default(mbcg_params* p) {
@@ -427,6 +446,7 @@ int mbcg_init(mbcg_case* c, mbcg_stream_t s) {
     if (!c) return fail(MBCG_E_INVALID, "null case");
     StepParams P = make_params(c, c->cur ^ 1, 0); // P.b = current state A
     MBCG_TRY(launch_init(c->p.precision, P, c->p, reinterpret_cast<cudaStream_t>(s)), "initial condition");
+    if (int rc = mirror_state(c, reinterpret_cast<cudaStream_t>(s))) return rc;
     c->steps = 0;
     return MBCG_OK;
 }
@@ -482,6 +502,12 @@ int mbcg_fields(const mbcg_case* c, mbcg_moments* a, mbcg_moments* b) {
 }
 
 int64_t mbcg_steps_done(const mbcg_case* c) { return c ? c->steps : -1; }
+
+int mbcg_case_params(const mbcg_case* c, mbcg_params* out) {
+    if (!c || !out) return fail(MBCG_E_INVALID, "null argument");
+    *out = c->p;
+    return MBCG_OK;
+}
 
 // Host copies move one whole dense field per transfer (one contiguous copy at full link
 // bandwidth: the reference's dense rows of nx floats would otherwise be copied row by row as a

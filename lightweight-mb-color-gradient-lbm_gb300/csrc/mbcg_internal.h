@@ -50,6 +50,11 @@ cudaError_t launch_from_dense(int precision, const StepParams& P, int field, con
 
 // sets the message mbcg_last_error() returns on the calling thread (mbcg_capi.cu)
 void set_last_error(const std::string& msg);
+// one field of a case's current state as dense FP32 (reference layout) into dst, on stream s;
+// the step counter of a case (restart from a checkpoint) (mbcg_capi.cu)
+int case_field_to_dense(mbcg_case* c, int field, float* dst, cudaStream_t s);
+int mirror_state(mbcg_case* c, cudaStream_t s); // current state -> the other (never-written layers agree)
+void case_set_steps(mbcg_case* c, long long steps);
 // parameter checks, the step's constant chain and TMA descriptors, shared by the case API and
 // the server (mbcg_capi.cu); validate_params sets the last-error message on failure
 int validate_params(const mbcg_params* p);

@@ -27,6 +27,8 @@ BC_PERIODIC, BC_INOUT, BC_WALL = 0, 1, 2
 OUTLET_CONVECTIVE, OUTLET_ZERO_GRADIENT = 0, 1
 FP32, FP16, BF16 = 0, 1, 2
 IC_JET, IC_BUBBLE, IC_RTI, IC_NONE = 0, 1, 2, 3
+VTI_ASCII, VTI_RAW = 0, 1
+VTI_REFERENCE_FIELDS = 0x1F
 
 
 class Params(ctypes.Structure):
@@ -302,6 +304,14 @@ _PROTOS = {
     "mbcg_copy_in": (ctypes.c_int, [_VP, _VP * NFIELDS, _VP]),
     "mbcg_diagnostics": (ctypes.c_int, [_VP, _P(Diag), _VP]),
     "mbcg_status": (ctypes.c_int, [_VP, _P(ctypes.c_int32)]),
+    "mbcg_case_params": (ctypes.c_int, [_VP, _P(Params)]),
+    "mbcg_write_vti": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int32, _VP]),
+    "mbcg_writer_create": (ctypes.c_int, [ctypes.c_int32, _P(_VP)]),
+    "mbcg_writer_snapshot": (ctypes.c_int, [_VP, _VP, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int32, _VP]),
+    "mbcg_writer_flush": (ctypes.c_int, [_VP]),
+    "mbcg_writer_destroy": (ctypes.c_int, [_VP]),
+    "mbcg_checkpoint_save": (ctypes.c_int, [_VP, ctypes.c_char_p, _VP]),
+    "mbcg_checkpoint_load": (ctypes.c_int, [ctypes.c_char_p, _P(_VP)]),
     "mbcg_get_shape": (ctypes.c_int, [_VP, _P(ctypes.c_int32), _P(ctypes.c_int32)]),
     "mbcg_set_shape": (ctypes.c_int, [_VP, ctypes.c_int32, ctypes.c_int32]),
     "mbcg_autotune": (ctypes.c_int, [_VP, ctypes.c_int32, _P(ctypes.c_double), _VP]),
@@ -367,12 +377,34 @@ def _stream_ptr(stream) -> Optional[int]:
 class Case:
     """Library-owned simulation state (mbcg_case*)."""
 
-    def __init__(self, params: Params, lib: Optional[Library] = None):
+    def __init__(self, params: Params, lib: Optional[Library] = None, _handle=None):
         self.lib = lib or Library.get()
         self.params = params.copy()
+        if _handle is not None:
+            self.handle = _handle
+            return
         h = ctypes.c_void_p()
         self.lib.check(self.lib.mbcg_create(ctypes.byref(self.params), ctypes.byref(h)), "mbcg_create")
         self.handle = h
+
+    @classmethod
+    def from_checkpoint(cls, path: str, lib: Optional[Library] = None) -> "Case":
+        """A case restored from mbcg_checkpoint_save's file: parameters, step count, state."""
+        lib = lib or Library.get()
+        h = ctypes.c_void_p()
+        lib.check(lib.mbcg_checkpoint_load(os.fsencode(path), ctypes.byref(h)), "mbcg_checkpoint_load")
+        p = Params()
+        lib.check(lib.mbcg_case_params(h, ctypes.byref(p)), "mbcg_case_params")
+        return cls(p, lib, _handle=h)
+
+    def checkpoint(self, path: str, stream=None):
+        self.lib.check(self.lib.mbcg_checkpoint_save(self.handle, os.fsencode(path), _stream_ptr(stream)),
+                       "mbcg_checkpoint_save")
+
+    def write_vti(self, path: str, fields: int = 0, fmt: int = VTI_ASCII, stream=None):
+        """State A as a VTI image (fields: bit mask over the 11 fields, 0 = the reference's five)."""
+        self.lib.check(self.lib.mbcg_write_vti(self.handle, os.fsencode(path), int(fields), int(fmt),
+                                               _stream_ptr(stream)), "mbcg_write_vti")
 
     def close(self):
         if getattr(self, "handle", None):
@@ -459,6 +491,64 @@ class Case:
         self.lib.check(self.lib.mbcg_autotune(self.handle, int(repeats), ctypes.byref(ms), _stream_ptr(stream)),
                        "mbcg_autotune")
         return float(ms.value)
+
+
+class Writer:
+    """Asynchronous VTI writer (mbcg_writer*): snapshots are taken on the case's stream and written
+    to disk while the case keeps stepping."""
+
+    def __init__(self, max_pending: int = 2, lib: Optional[Library] = None):
+        self.lib = lib or Library.get()
+        h = ctypes.c_void_p()
+        self.lib.check(self.lib.mbcg_writer_create(int(max_pending), ctypes.byref(h)), "mbcg_writer_create")
+        self.handle = h
+
+    def snapshot(self, case: Case, path: str, fields: int = 0, fmt: int = VTI_RAW, stream=None):
+        self.lib.check(self.lib.mbcg_writer_snapshot(self.handle, case.handle, os.fsencode(path), int(fields),
+                                                     int(fmt), _stream_ptr(stream)), "mbcg_writer_snapshot")
+
+    def flush(self):
+        self.lib.check(self.lib.mbcg_writer_flush(self.handle), "mbcg_writer_flush")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            rc = self.lib.mbcg_writer_destroy(self.handle)
+            self.handle = None
+            self.lib.check(rc, "mbcg_writer_destroy")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def read_vti(path: str) -> dict:
+    """Fields of a VTI image written by mbcg_write_vti / Writer (ASCII or appended raw) as float32
+    arrays of shape (nz, ny, nx), keyed by name."""
+    import re
+    data = open(path, "rb").read()
+    head_end = data.find(b"<AppendedData")
+    text = data[: head_end if head_end >= 0 else len(data)].decode()
+    ext = [int(v) for v in re.search(r'WholeExtent="([^"]+)"', text).group(1).split()]
+    shape = (ext[5] + 1, ext[3] + 1, ext[1] + 1)
+    out = {}
+    if head_end >= 0:
+        start = data.index(b"_", head_end) + 1
+        for name, off in re.findall(r'Name="(\w+)" format="appended" offset="(\d+)"', text):
+            o = start + int(off)
+            nbytes = int(np.frombuffer(data[o:o + 8], dtype=np.uint64)[0])
+            out[name] = np.frombuffer(data[o + 8:o + 8 + nbytes], dtype=np.float32).reshape(shape)
+    else:
+        for name, body in re.findall(r'Name="(\w+)" format="ascii">\n(.*?)</DataArray>', text, flags=re.S):
+            out[name] = np.array(body.split(), dtype=np.float32).reshape(shape)
+    return out
 
 
 def server_config(**kw) -> ServerConfig:

@@ -97,14 +97,57 @@ def ic_fixture():
     save("ref_ic", p, bubble=sh.init("bubble"), rti=sh.init("rti"))
 
 
+def vti_state(p: mbcg.Params) -> np.ndarray:
+    """Seeded FP32 state with values of many magnitudes and both signs, every one exactly
+    representable (small integers times powers of two and a decimal scale, formed in float32);
+    the periodic ghost layers of x and y hold the images of the opposite fluid layer, as the
+    library keeps them."""
+    rng = np.random.default_rng(77)
+    s = np.zeros((11,) + p.shape, dtype=np.float32)
+    scale = [np.float32(v) for v in (1.0, 1e-3, 1e-7, 3.5e2, 1e-20)]
+    for f in range(11):
+        ints = rng.integers(-100000, 100000, p.shape).astype(np.float32) * np.float32(2.0 ** -12)
+        s[f] = ints * scale[f % len(scale)]
+    s[:, :, :, 0] = s[:, :, :, p.nx - 2]
+    s[:, :, :, p.nx - 1] = s[:, :, :, 1]
+    s[:, :, 0, :] = s[:, :, p.ny - 2, :]
+    s[:, :, p.ny - 1, :] = s[:, :, 1, :]
+    return s
+
+
+def vti_fixture():
+    """The reference's own VTI writer (io/vtiWriter.cuh, write_vti) on a seeded state: the bytes
+    the library's ASCII writer must reproduce."""
+    import subprocess
+    import tempfile
+    p = mbcg.bubble_params(5, q=19)  # 7 x 7 x 7 lattice, periodic
+    p.nx, p.ny, p.nz = 9, 7, 6
+    p.ic = mbcg.IC_NONE
+    s = vti_state(p)
+    defs = " ".join(ol.shim_defs(p, "float"))
+    subprocess.run(["make", "-s", "-C", ol.ORACLE_DIR, "vti", "TAG=golden", f"DEFS={defs}",
+                    f"REF_ROOT={ol.REF_ROOT}"], check=True)
+    with tempfile.TemporaryDirectory() as d:
+        raw = os.path.join(d, "in.raw")
+        s[0:5].astype(np.float32).tofile(raw)
+        out = os.path.join(HERE, "ref_vti_ascii.vti")
+        subprocess.run([os.path.join(ol.REF_DIR, "ref_vti_golden"), raw, out], check=True, capture_output=True)
+    save("ref_vti_state", p, state=s)
+    print("wrote", out)
+
+
 def main():
     if not ol.reference_available():
         raise SystemExit("reference sources not found; set MBCG_REF_ROOT")
+    if len(sys.argv) > 1 and sys.argv[1] == "vti":
+        vti_fixture()
+        return
     for q in (27, 19):
         jet_fixture(q)
         random_fixture(q)
     defaults_fixture()
     ic_fixture()
+    vti_fixture()
 
 
 if __name__ == "__main__":

@@ -73,3 +73,14 @@ def test_initial_conditions_bitexact():
     np.testing.assert_array_equal(ol.oracle_init(p, np.float32), z["bubble"])
     p.ic = mbcg.IC_RTI
     np.testing.assert_array_equal(ol.oracle_init(p, np.float32), z["rti"])
+
+
+def test_vti_golden_holds_the_fixture_state():
+    """The reference writer's golden VTI holds the seeded state it was written from (checks the
+    fixture pair and the VTI reader on the CPU)."""
+    import mbcg
+    z = np.load(os.path.join(GOLD, "ref_vti_state.npz"))
+    got = mbcg.read_vti(os.path.join(GOLD, "ref_vti_ascii.vti"))
+    assert list(got) == ["rhor", "rhob", "ux", "uy", "uz"]
+    for f, name in enumerate(got):
+        np.testing.assert_array_equal(got[name], z["state"][f])
