@@ -200,6 +200,30 @@ def cpu_leg(budget_s: float, threads: int, real_bytes: int = 4) -> dict:
 
 
 # ---------------------------------------------------------------- serving workload
+# ---------------------------------------------------------------- the other configurations
+def configs_leg(torch) -> dict:
+    """MLUPS of the plain step on the other configurations (state resident, launch shape measured
+    by mbcg_autotune first): the 64^3 D3Q19 periodic bubble (config 0 physics), the
+    128 x 128 x 512 D3Q27 Rayleigh-Taylor box (config 1 physics) and the jet in D3Q19."""
+    cases = {
+        "bubble64_q19": (mbcg.bubble_params(64, q=19), 400),
+        "rti128x512_q27": (mbcg.rti_params(128, q=27), 100),
+        "jet256x1024_q19": (mbcg.jet_params(256, 256, 1024, q=19), 50),
+    }
+    out = {}
+    for name, (p, steps) in cases.items():
+        with mbcg.Case(p) as c:
+            c.init()
+            c.autotune(repeats=3)
+            ms = time_device(c, steps, 3, torch) / steps * 1e3
+            w, z = c.shape
+        state_bytes = 2 * 11 * 4 * p.nx * p.ny * p.nz
+        out[name] = {"mlups": p.active_nodes() / ms / 1e3, "ms_per_step": ms, "block_rows": w, "zchunk": z,
+                     "roofline_frac": BYTES_PER_NODE[mbcg.FP32] * p.active_nodes() / (ms * 1e-3) / 1e9 / measured_peak_hbm()[0],
+                     "state_bytes": state_bytes, "l2_resident": state_bytes < 129e6}
+    return out
+
+
 def serving_requests(n: int, rate: float, step_scale: float, seed: int = 20240):
     """Seeded request stream: Poisson arrivals at `rate`/s; bubble (config-0 physics, radius L/4,
     L log-uniform in [32, 192]) or Rayleigh-Taylor (config-1 physics, L x L x 4L, L log-uniform
@@ -336,6 +360,7 @@ def main() -> None:
     ap.add_argument("--forms", default="fp16,bf16")
     ap.add_argument("--nz", type=int, default=1024, help="fluid planes of the jet (profiling uses fewer)")
     ap.add_argument("--serving", default="sample", choices=["off", "sample", "full"])
+    ap.add_argument("--no-configs", action="store_true", help="skip the bubble / RTI / D3Q19 lines")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -388,6 +413,7 @@ def main() -> None:
 
     e2e = time_e2e(p, args.e2e_steps, torch) if rank == 0 and args.e2e_steps > 0 else None
     serving = serving_leg(args.serving, torch) if rank == 0 and args.serving != "off" else None
+    configs = configs_leg(torch) if rank == 0 and not args.no_configs else None
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_leg(args.cpu_budget, os.cpu_count() or 1)
@@ -406,6 +432,7 @@ def main() -> None:
                          "algorithmic_bytes_per_node": BYTES_PER_NODE[mbcg.FP32]},
             "forms": forms,
             "serving": serving,
+            "configs": configs,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps * launches,

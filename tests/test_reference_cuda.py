@@ -4,7 +4,8 @@ the GPU beside this library.
 
 * parity: the reference's RCSKernel + JetBoundaryConditions from the golden jet fixture's
   initial state agree with the reference's host build (the fixture) and with libmbcg.so;
-* timing: the reference kernel on the 256 x 1024 x 256 jet (printed; run with -s).
+* timing: the reference kernel on the 256 x 1024 x 256 jet and at the bubble's and the Rayleigh-Taylor
+  case's sizes, beside this library on the same lattices (printed; run with -s).
 
 Skipped when the cubins are absent (the reference sources are not available everywhere).
 """
@@ -98,12 +99,23 @@ def test_reference_cuda_matches_host_build_and_library(q):
             assert e_ours["rhor"] < 1e-5 and e_ours["rhob"] < 1e-5, (n, e_ours)
 
 
-def test_reference_cuda_timing_jet256():
-    """Prints the reference kernel's MLUPS on the 256 x 1024 x 256 jet (no assertion on speed)."""
+REF_TIMING = {
+    # tag: (lattice, q, steps) -- the jet (256 x 1024 x 256 fluid nodes), and the reference kernel at
+    # the bubble's (64^3, D3Q19) and the Rayleigh-Taylor case's (128 x 512 x 128, D3Q27) sizes
+    "jet256": ((258, 1026, 258), 27, 20),
+    "box64_q19": ((66, 66, 66), 19, 200),
+    "box128x512_q27": ((130, 514, 130), 27, 50),
+}
+
+
+@pytest.mark.parametrize("tag", sorted(REF_TIMING))
+def test_reference_cuda_timing(tag):
+    """Prints the reference kernel's MLUPS at each configuration's size and this library's on the
+    same lattice (no assertion on speed)."""
     import torch
-    NX, NY, NZ = 258, 1026, 258
-    k = RefKernels(_cubin("jet256"), (NX, NY, NZ))
-    p = mbcg.reference_jet_params(NX, NY, NZ, q=27, tau=0.51, sigma=1e-3, beta=0.7, radius=16.0)
+    (NX, NY, NZ), q, steps = REF_TIMING[tag]
+    k = RefKernels(_cubin(tag), (NX, NY, NZ))
+    p = mbcg.reference_jet_params(NX, NY, NZ, q=q, tau=0.51, sigma=1e-3, beta=0.7, radius=16.0)
     lib = mbcg.Library.get()
     a = [torch.zeros(NX * NY * NZ, device="cuda") for _ in range(11)]
     m = mbcg.moments_from_tensors(a, NX)
@@ -114,7 +126,6 @@ def test_reference_cuda_timing_jet256():
         a, b = b, a
     torch.cuda.synchronize()
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    steps = 20
     s.record()
     for i in range(steps):
         k.step(a, b)
@@ -122,6 +133,17 @@ def test_reference_cuda_timing_jet256():
     e.record()
     torch.cuda.synchronize()
     ms = s.elapsed_time(e) / steps
-    mlups = (NX - 2) * (NY - 2) * (NZ - 2) / ms / 1e3
-    print(f"\nreference RCSKernel + JetBoundaryConditions, 256x1024x256 fluid nodes: {ms:.3f} ms/step, {mlups:.0f} MLUPS")
+    nodes = (NX - 2) * (NY - 2) * (NZ - 2)
+    mlups = nodes / ms / 1e3
+    with mbcg.Case(p) as c:
+        c.init()
+        c.step(3)
+        torch.cuda.synchronize()
+        s.record()
+        c.step(steps)
+        e.record()
+        torch.cuda.synchronize()
+        ms_ours = s.elapsed_time(e) / steps
+    print(f"\nreference RCSKernel + JetBoundaryConditions, {tag} ({NX - 2}x{NY - 2}x{NZ - 2} fluid nodes, D3Q{q}): "
+          f"{ms:.3f} ms/step, {mlups:.0f} MLUPS; this library on the same lattice {nodes / ms_ours / 1e3:.0f} MLUPS")
     assert mlups > 0
