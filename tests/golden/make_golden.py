@@ -136,11 +136,66 @@ def vti_fixture():
     print("wrote", out)
 
 
+OPS_LATTICE = dict(nx=9, ny=8, nz=7)
+
+
+def ops_params(q: int) -> mbcg.Params:
+    """The configuration the operator fixtures are evaluated at (a reference-expressible jet
+    along y on a 9 x 8 x 7 lattice)."""
+    p = mbcg.reference_jet_params(OPS_LATTICE["nx"], OPS_LATTICE["ny"], OPS_LATTICE["nz"], q=q, tau=0.8,
+                                  sigma=0.05, beta=0.7, radius=2.0, velocity=0.05)
+    p.bubble_radius = 2.5
+    p.rti_amplitude = 1.0
+    p.rti_width = 1.5
+    return p
+
+
+def ops_inputs(p: mbcg.Params, seed: int = 5) -> np.ndarray:
+    """Seeded float32 inputs of tests/cpp/ops_eval.cpp: 32 samples of (rho, u, Pi, F, rhor, rhob),
+    with the force vectors spanning both sides of the |F| = 1e-4 cut-off, then two lattice states."""
+    rng = np.random.default_rng(seed)
+    ns = 32
+    smp = np.zeros((ns, 15))
+    smp[:, 0] = rng.uniform(0.8, 1.2, ns)
+    smp[:, 1:4] = rng.uniform(-0.06, 0.06, (ns, 3))
+    smp[:, 4:10] = rng.uniform(-3e-3, 3e-3, (ns, 6))
+    mag = 10.0 ** rng.uniform(-6, -1, ns)
+    smp[:, 10:13] = rng.normal(size=(ns, 3)) * mag[:, None]
+    smp[:, 13] = rng.uniform(0.0, 1.0, ns)
+    smp[:, 14] = rng.uniform(0.0, 1.0, ns)
+    smp[0, 13] = 0.0  # a pure blue node
+    states = [random_mixed_state(p, seed + 1 + i, np.float32) for i in range(2)]
+    return np.concatenate([smp.astype(np.float32).ravel()] + [s.ravel() for s in states])
+
+
+def ops_fixture(q: int):
+    """The reference's own operator headers evaluated by tests/cpp/ops_eval.cpp (-DOPS_REFERENCE)
+    on seeded inputs: what include/mbcg_operators.cuh must reproduce bit for bit."""
+    import subprocess
+    import tempfile
+    p = ops_params(q)
+    inp = ops_inputs(p)
+    tag = f"ops{q}"
+    defs = " ".join(ol.shim_defs(p, "float"))
+    subprocess.run(["make", "-s", "-C", ol.ORACLE_DIR, "ops", f"TAG={tag}", f"DEFS={defs}",
+                    f"REF_ROOT={ol.REF_ROOT}"], check=True)
+    with tempfile.TemporaryDirectory() as d:
+        fi, fo = os.path.join(d, "in.raw"), os.path.join(d, "out.raw")
+        inp.tofile(fi)
+        subprocess.run([os.path.join(ol.REF_DIR, f"ops_ref_{tag}"), fi, fo], check=True)
+        out = np.fromfile(fo, dtype=np.float32)
+    save(f"ref_ops_q{q}", p, inputs=inp, outputs=out)
+
+
 def main():
     if not ol.reference_available():
         raise SystemExit("reference sources not found; set MBCG_REF_ROOT")
     if len(sys.argv) > 1 and sys.argv[1] == "vti":
         vti_fixture()
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "ops":
+        for q in (27, 19):
+            ops_fixture(q)
         return
     for q in (27, 19):
         jet_fixture(q)
@@ -148,6 +203,8 @@ def main():
     defaults_fixture()
     ic_fixture()
     vti_fixture()
+    for q in (27, 19):
+        ops_fixture(q)
 
 
 if __name__ == "__main__":
