@@ -172,6 +172,33 @@ int mbcg_status(mbcg_case *c, int32_t *status);
 /* The parameters the case was created with. */
 int mbcg_case_params(const mbcg_case *c, mbcg_params *out);
 
+/* ---- in-situ phase statistics (no counterpart in the reference) ---------------------- */
+/* The "tracked" phase is the injected one for a jet (the sign of jet_phase), else red
+ * (phi > 0).  FP64 sums over the fluid nodes of state A, computed on the GPU. */
+typedef struct mbcg_phase_stats {
+    double volume_tracked;      /* fluid nodes where the tracked phase dominates (its phi > 0)   */
+    double volume_other;
+    double interface_area;      /* sum of |grad phi| / 2 (central differences): the area of a
+                                   diffuse interface of any profile, in lattice units^2          */
+    int64_t interface_nodes;    /* 4 rho_r rho_b / rho^2 > 1e-4 (lbm.cuh:181)                    */
+    double penetration;         /* inlet/outlet axis: largest distance from the inlet ghost layer
+                                   of a node where the tracked phase dominates; -1 otherwise      */
+    double centroid[3];         /* centroid of the tracked phase (fluid-node coordinates)        */
+    /* MBCG_STATS_COMPONENTS only (else -1): regions of the tracked phase connected through
+     * faces, periodic axes wrapped */
+    int64_t components;
+    int64_t largest_component;  /* nodes in the largest region                                  */
+    int64_t detached;           /* regions not touching the first fluid layer of the inlet axis
+                                   (all regions without one): droplets                          */
+    int64_t detached_volume;    /* nodes in them                                                */
+    int32_t status;             /* non-zero: a bounded device loop gave up (results incomplete) */
+    int32_t reserved;
+} mbcg_phase_stats;
+
+#define MBCG_STATS_COMPONENTS 1 /* also label connected regions (temporary: 8 bytes per node) */
+
+int mbcg_phase_statistics(mbcg_case *c, int32_t flags, mbcg_phase_stats *out, mbcg_stream_t s);
+
 /* ---- output: VTI images (io/vtiWriter.cuh:60-164) and checkpoints ---------------------- */
 #define MBCG_VTI_ASCII 0   /* the reference's encoding: Float32 ASCII DataArrays, "%.8e " per value,
                               one x row per line (io/vtiWriter.cuh:60-85)                      */

@@ -331,6 +331,12 @@ int mbcg::mirror_state(mbcg_case* c, cudaStream_t s) {
     return MBCG_OK;
 }
 
+int mbcg::case_state_params(mbcg_case* c, StepParams* out) {
+    if (!c || !out) return fail(MBCG_E_INVALID, "null argument");
+    *out = make_params(c, c->cur, c->steps); // P.a = current state
+    return MBCG_OK;
+}
+
 int mbcg::case_field_to_dense(mbcg_case* c, int field, float* dst, cudaStream_t s) {
     if (!c || !dst || field < 0 || field >= NF) return fail(MBCG_E_INVALID, "bad field snapshot request");
     StepParams P = make_params(c, c->cur, c->steps); // P.a = current state

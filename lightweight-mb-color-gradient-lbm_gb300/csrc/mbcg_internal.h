@@ -53,6 +53,7 @@ void set_last_error(const std::string& msg);
 // one field of a case's current state as dense FP32 (reference layout) into dst, on stream s;
 // the step counter of a case (restart from a checkpoint) (mbcg_capi.cu)
 int case_field_to_dense(mbcg_case* c, int field, float* dst, cudaStream_t s);
+int case_state_params(mbcg_case* c, StepParams* out); // parameter block with P.a = current state
 int mirror_state(mbcg_case* c, cudaStream_t s); // current state -> the other (never-written layers agree)
 void case_set_steps(mbcg_case* c, long long steps);
 // parameter checks, the step's constant chain and TMA descriptors, shared by the case API and

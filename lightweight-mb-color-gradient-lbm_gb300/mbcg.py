@@ -240,6 +240,24 @@ class Diag(ctypes.Structure):
                 "nonfinite": self.nonfinite, "nodes": self.nodes}
 
 
+class PhaseStats(ctypes.Structure):
+    """Mirror of ``mbcg_phase_stats``."""
+    _fields_ = [("volume_tracked", ctypes.c_double), ("volume_other", ctypes.c_double),
+                ("interface_area", ctypes.c_double), ("interface_nodes", ctypes.c_int64),
+                ("penetration", ctypes.c_double), ("centroid", ctypes.c_double * 3),
+                ("components", ctypes.c_int64), ("largest_component", ctypes.c_int64),
+                ("detached", ctypes.c_int64), ("detached_volume", ctypes.c_int64),
+                ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        d = {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+        d["centroid"] = list(self.centroid)
+        return d
+
+
+STATS_COMPONENTS = 1
+
+
 class ServerConfig(ctypes.Structure):
     """Mirror of ``mbcg_server_config``."""
     _fields_ = [("arena_bytes", ctypes.c_int64), ("max_live", ctypes.c_int32), ("chunk_steps", ctypes.c_int32),
@@ -305,6 +323,7 @@ _PROTOS = {
     "mbcg_diagnostics": (ctypes.c_int, [_VP, _P(Diag), _VP]),
     "mbcg_status": (ctypes.c_int, [_VP, _P(ctypes.c_int32)]),
     "mbcg_case_params": (ctypes.c_int, [_VP, _P(Params)]),
+    "mbcg_phase_statistics": (ctypes.c_int, [_VP, ctypes.c_int32, _P(PhaseStats), _VP]),
     "mbcg_write_vti": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int32, _VP]),
     "mbcg_writer_create": (ctypes.c_int, [ctypes.c_int32, _P(_VP)]),
     "mbcg_writer_snapshot": (ctypes.c_int, [_VP, _VP, ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int32, _VP]),
@@ -400,6 +419,14 @@ class Case:
     def checkpoint(self, path: str, stream=None):
         self.lib.check(self.lib.mbcg_checkpoint_save(self.handle, os.fsencode(path), _stream_ptr(stream)),
                        "mbcg_checkpoint_save")
+
+    def phase_statistics(self, components: bool = False, stream=None) -> dict:
+        """In-situ phase statistics of state A (volumes, interface area, penetration, regions)."""
+        st = PhaseStats()
+        self.lib.check(self.lib.mbcg_phase_statistics(self.handle, STATS_COMPONENTS if components else 0,
+                                                      ctypes.byref(st), _stream_ptr(stream)),
+                       "mbcg_phase_statistics")
+        return st.as_dict()
 
     def write_vti(self, path: str, fields: int = 0, fmt: int = VTI_ASCII, stream=None):
         """State A as a VTI image (fields: bit mask over the 11 fields, 0 = the reference's five)."""

@@ -53,7 +53,8 @@ def _c_layout(struct, fields):
 @pytest.mark.parametrize("pyt,cname", [(mbcg.Params, "mbcg_params"), (mbcg.Moments, "mbcg_moments"),
                                        (mbcg.Diag, "mbcg_diag"), (mbcg.ServerConfig, "mbcg_server_config"),
                                        (mbcg.RequestInfo, "mbcg_request_info"),
-                                       (mbcg.ServerStats, "mbcg_server_stats")])
+                                       (mbcg.ServerStats, "mbcg_server_stats"),
+                                       (mbcg.PhaseStats, "mbcg_phase_stats")])
 def test_struct_layout_matches_c(pyt, cname):
     names = [n for n, _ in pyt._fields_]
     c = _c_layout(cname, names)
