@@ -198,6 +198,9 @@ typedef struct mbcg_phase_stats {
 #define MBCG_STATS_COMPONENTS 1 /* also label connected regions (temporary: 8 bytes per node) */
 
 int mbcg_phase_statistics(mbcg_case *c, int32_t flags, mbcg_phase_stats *out, mbcg_stream_t s);
+/* The same on caller-owned arrays (reference layout, any pitch >= nx). */
+int mbcg_phase_statistics_moments(const mbcg_params *p, const mbcg_moments *a, int32_t flags,
+                                  mbcg_phase_stats *out, mbcg_stream_t s);
 
 /* ---- output: VTI images (io/vtiWriter.cuh:60-164) and checkpoints ---------------------- */
 #define MBCG_VTI_ASCII 0   /* the reference's encoding: Float32 ASCII DataArrays, "%.8e " per value,

@@ -310,4 +310,42 @@ inline void write_vti_step_device(int step, const MomentsDevice& d, LbmHost& h, 
     write_vti(vti_filename(step, folder), h, cfg.params);
 }
 
+// ------------------------------------------------------------------ jet-breakup statistics
+// The reference declares a statistics sampler's interval and start (NSTATS_SAMPLE = 20,
+// stats_start_tstar = 7000: constants.cuh:11,53) but implements none.  This one records the
+// in-situ phase statistics (mbcg_phase_statistics_moments, connected regions included) of a
+// state every `every` steps from step `start` on, one CSV row per sample: the jet's penetration,
+// its number of regions, the detached droplets and their volume, the largest region, the
+// interface area and node count, and the injected phase's volume.
+class JetBreakupSampler {
+  public:
+    JetBreakupSampler(const std::filesystem::path& csv, int every = 20, long long start = 7000)
+        : every_(every > 0 ? every : 1), start_(start) {
+        if (!csv.parent_path().empty()) std::filesystem::create_directories(csv.parent_path());
+        out_.open(csv);
+        if (!out_) throw mbcg::Error("Cannot open statistics file: " + csv.string());
+        out_ << "step,penetration,regions,detached,detached_volume,largest_region,interface_area,"
+                "interface_nodes,injected_volume\n";
+    }
+    // samples the state if step is due; returns whether it did
+    bool sample(long long step, const MomentsDevice& A, const CudaConfig& cfg) {
+        if (step < start_ || (step - start_) % every_ != 0) return false;
+        const mbcg_moments m = to_view(A, cfg.params);
+        mbcg_phase_stats st;
+        mbcg::check(mbcg_phase_statistics_moments(&cfg.params, &m, MBCG_STATS_COMPONENTS, &st,
+                                                  reinterpret_cast<mbcg_stream_t>(cfg.stream)),
+                    "phase statistics");
+        out_ << step << ',' << st.penetration << ',' << st.components << ',' << st.detached << ','
+             << st.detached_volume << ',' << st.largest_component << ',' << std::setprecision(10)
+             << st.interface_area << ',' << st.interface_nodes << ',' << st.volume_tracked << '\n';
+        out_.flush();
+        return true;
+    }
+
+  private:
+    int every_;
+    long long start_;
+    std::ofstream out_;
+};
+
 #endif // MBCG_LBM_HPP

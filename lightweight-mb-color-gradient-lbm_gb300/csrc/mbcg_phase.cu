@@ -215,15 +215,10 @@ cudaError_t sums(const PhaseArgs& A, double* partials, int nparts, double* resul
     return cudaGetLastError();
 }
 
-} // namespace
-
-extern "C" int mbcg_phase_statistics(mbcg_case* c, int32_t flags, mbcg_phase_stats* out, mbcg_stream_t s) {
-    if (!c || !out) return fail(MBCG_E_INVALID, "null argument");
-    mbcg_params p;
-    if (int rc = mbcg_case_params(c, &p)) return rc;
+int phase_statistics(const mbcg_params& p, const StepParams& P, int32_t flags, mbcg_phase_stats* out, mbcg_stream_t s) {
     PhaseArgs A;
     std::memset(&A, 0, sizeof(A));
-    if (int rc = case_state_params(c, &A.P)) return rc;
+    A.P = P;
     A.ia = A.P.inout_axis;
     A.sign = (A.ia >= 0 && p.ic == MBCG_IC_JET && p.jet_phase < 0.0) ? -1 : 1;
     A.nf[0] = p.nx - 2;
@@ -299,3 +294,33 @@ extern "C" int mbcg_phase_statistics(mbcg_case* c, int32_t flags, mbcg_phase_sta
     out->status = stat;
     return MBCG_OK;
 }
+
+} // namespace
+
+extern "C" {
+
+int mbcg_phase_statistics(mbcg_case* c, int32_t flags, mbcg_phase_stats* out, mbcg_stream_t s) {
+    if (!c || !out) return fail(MBCG_E_INVALID, "null argument");
+    mbcg_params p;
+    if (int rc = mbcg_case_params(c, &p)) return rc;
+    StepParams P;
+    if (int rc = case_state_params(c, &P)) return rc;
+    return phase_statistics(p, P, flags, out, s);
+}
+
+int mbcg_phase_statistics_moments(const mbcg_params* p, const mbcg_moments* a, int32_t flags, mbcg_phase_stats* out,
+                                  mbcg_stream_t s) {
+    if (!p || !a || !out) return fail(MBCG_E_INVALID, "null argument");
+    if (int rc = validate_params(p)) return rc;
+    if (a->precision != p->precision || a->pitch < p->nx) return fail(MBCG_E_INVALID, "moments do not match params");
+    for (int i = 0; i < NF; ++i)
+        if (!a->f[i]) return fail(MBCG_E_INVALID, "null field pointer");
+    StepParams P;
+    fill_step_physics(*p, P);
+    P.pitch = a->pitch;
+    P.plane = a->pitch * p->ny;
+    for (int i = 0; i < NF; ++i) P.a[i] = a->f[i];
+    return phase_statistics(*p, P, flags, out, s);
+}
+
+} // extern "C"

@@ -1,8 +1,9 @@
 // A driver written against the reference's host API names (include/mbcg_lbm.hpp), following
 // the reference's main loop (main.cu:25-55): allocate, initialise the jet, then RCS, jet
-// boundary conditions and swap per step, with the MLUPS counter; prints per-field sums and sums of
-// magnitudes.
+// boundary conditions and swap per step, with the MLUPS counter and optionally the jet-breakup
+// statistics sampler; prints per-field sums and sums of magnitudes.
 #include <cstdio>
+#include <memory>
 #include <vector>
 
 #include "mbcg_lbm.hpp"
@@ -18,12 +19,19 @@ int main(int argc, char** argv) {
     LbmDevice d = allocate_device_memory(cfg);
     launch_InitJet(d.A, cfg);
     MlupsCounter mlups = make_mlups_counter(mlups_active_cells(p));
+    // optional jet-breakup statistics (every 5 steps from step 5) into the CSV named by argv[2]
+    std::unique_ptr<JetBreakupSampler> sampler;
+    if (argc > 2) sampler = std::make_unique<JetBreakupSampler>(argv[2], 5, 5);
     mlups_start(mlups);
     for (int step = 1; step <= steps; ++step) {
         launch_RCS(d.A, d.B, cfg, step);
         launch_JetBoundaryConditions(d.B, d.A, cfg, step);
         swap_moments(d.A, d.B);
         mlups_count_step(mlups);
+        if (sampler) {
+            MlupsPause pause(mlups); // statistics are not timed, as the reference's output is not
+            sampler->sample(step, d.A, cfg);
+        }
     }
     mlups_stop(mlups);
     const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;

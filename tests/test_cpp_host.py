@@ -45,3 +45,22 @@ def test_reference_api_driver_matches_case_api(tmp_path):
     # of the velocity fields cancel to ~1e-7 and carry no relative precision of their own).
     for a, b, m in zip(out["sums"], sums, out["abs_sums"]):
         assert abs(a - b) <= 1e-5 * m + 1e-12, (out["sums"], sums)
+
+
+@pytest.mark.gpu
+def test_jet_breakup_sampler_records_statistics(tmp_path):
+    """JetBreakupSampler (include/mbcg_lbm.hpp) in the reference-style loop: one CSV row every 5
+    steps from step 5, the injected jet attached to the inlet and advancing."""
+    exe = build_driver(tmp_path)
+    csv = os.path.join(str(tmp_path), "stats", "jet.csv")
+    subprocess.run([exe, "40", csv], check=True, capture_output=True, text=True)
+    rows = [line.split(",") for line in open(csv).read().strip().splitlines()]
+    head, data = rows[0], rows[1:]
+    assert head[:4] == ["step", "penetration", "regions", "detached"]
+    steps = [int(r[0]) for r in data]
+    assert steps == list(range(5, 41, 5))
+    pen = [float(r[1]) for r in data]
+    assert all(b >= a for a, b in zip(pen, pen[1:])) and pen[-1] > pen[0] >= 1
+    for r in data:
+        regions, detached, largest = int(r[2]), int(r[3]), int(r[5])
+        assert regions >= 1 and 0 <= detached < regions and largest > 0
