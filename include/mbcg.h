@@ -106,6 +106,12 @@ typedef struct mbcg_params {
     double rho_scale;       /* (rho - rho_nominal) / rho_scale is stored; default 0.01     */
     double u_ref;           /* u / u_ref is stored; default 0.05                           */
     double pi_scale;        /* Pi / pi_scale is stored; default u_ref^2                    */
+    /* phase-dependent relaxation (forces.cuh:101-108, defined but unused by the reference):
+       0 (reference) = one relaxation time tau for both phases; > 0 = tau is the red phase's and
+       tau_b the blue phase's, blended per node as tau_interface does,
+       tau_eff = (1 + psi)/2 tau + (1 - psi)/2 tau_b, which sets oms = 1 - 1/tau_eff and the
+       Omega2 amplitude sigma / (4 cs^4 tau_eff) at that node                               */
+    double tau_b;
 } mbcg_params;
 
 /* Fill *p with the reference's shipped constants (constants.cuh:9-93): D3Q27, 128^3 jet

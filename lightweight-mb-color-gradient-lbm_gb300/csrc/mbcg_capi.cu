@@ -56,6 +56,7 @@ int validate(const mbcg_params* p) {
     if (nonper > 1) return fail(MBCG_E_INVALID, "at most one axis may be non-periodic");
     if (p->precision < MBCG_FP32 || p->precision > MBCG_BF16) return fail(MBCG_E_INVALID, "unknown precision");
     if (!(p->tau > 0.5)) return fail(MBCG_E_INVALID, "tau must exceed 1/2");
+    if (p->tau_b != 0.0 && !(p->tau_b > 0.5)) return fail(MBCG_E_INVALID, "tau_b must be 0 or exceed 1/2");
     if (!(p->rho_r0 > 0.0) || !(p->rho_b0 > 0.0)) return fail(MBCG_E_INVALID, "phase densities must be positive");
     if (p->precision != MBCG_FP32 && (!(p->rho_scale > 0) || !(p->u_ref > 0) || !(p->pi_scale > 0)))
         return fail(MBCG_E_INVALID, "FP16/BF16 storage needs positive rho_scale, u_ref and pi_scale");
@@ -83,6 +84,10 @@ void fill_physics(const mbcg_params& p, StepParams& P) {
     const float cs4 = cs2 * cs2;
     const float s4 = static_cast<float>(p.sigma) / (4.0f * cs4);
     P.A = s4 / taub;
+    P.s4 = s4;
+    P.tau_var = p.tau_b > 0.0 && p.tau_b != p.tau;
+    P.tau_r = taub;
+    P.tau_b = p.tau_b > 0.0 ? static_cast<float>(p.tau_b) : taub;
     P.beta = static_cast<float>(p.beta);
     P.omega2_conservative = p.omega2_conservative != 0;
     P.ratio = p.rho_r0 != p.rho_b0;

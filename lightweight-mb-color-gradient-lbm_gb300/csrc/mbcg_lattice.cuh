@@ -129,6 +129,8 @@ struct StepParams {
     // collision
     float oms;          // 1 - 1/tau (constants.cuh:85)
     float A;            // sigma / (4 cs^4 tau) (forces.cuh:114-117, 132-134)
+    int tau_var;        // phase-dependent relaxation: tau_eff = (1+psi)/2 tau_r + (1-psi)/2 tau_b
+    float tau_r, tau_b, s4; // s4 = sigma / (4 cs^4), so A = s4 / tau_eff
     float beta;
     int omega2_conservative; // Omega2 = 0 below |F| = 1e-4 (mass conserving option)
     int ratio;          // density-ratio rest population on
@@ -154,15 +156,15 @@ struct StepParams {
     void* b[NF];        // next state
 };
 
-// Optional parts of the step a lattice needs: bounce-back walls, a body force or density-ratio
-// rest term, an inlet/outlet axis.  Kernels are instantiated per feature set.
+// Optional parts of the step a lattice needs: bounce-back walls, a body force, density-ratio rest
+// term or phase-dependent relaxation time (F_FORCE), an inlet/outlet axis.  Kernels are instantiated per feature set.
 constexpr int F_WALL = 1, F_FORCE = 2, F_INOUT = 4, F_ALL = 7;
 
 MBCG_HD int features_of(const StepParams& P) {
     int f = 0;
     for (int a = 0; a < 3; ++a)
         if (P.bc[a] == MBCG_BC_WALL) f |= F_WALL;
-    if (P.forced || P.ratio) f |= F_FORCE;
+    if (P.forced || P.ratio || P.tau_var) f |= F_FORCE;
     if (P.inout_axis >= 0) f |= F_INOUT;
     return f;
 }

@@ -233,11 +233,19 @@ struct Coef {
 // Equilibrium (pdf.cuh:16-36) at (rho, u) + oms * regularised non-equilibrium (pdf.cuh:38-79)
 // from (Pi, v) + 1/2 Guo force (pdf.cuh:94-136) + density-ratio rest term, as the
 // coefficients of a polynomial in c (w_i factored out).
+// Phase-dependent relaxation (forces.cuh:101-108): tau_eff = (1 + psi)/2 tau_r + (1 - psi)/2 tau_b
+__device__ __forceinline__ float tau_eff_of(const StepParams& P, float rr, float rb) {
+    const float psix = (rr - rb) / (rr + rb);
+    return 0.5f * (1.0f + psix) * P.tau_r + 0.5f * (1.0f - psix) * P.tau_b;
+}
+
 template <int kFeat>
 __device__ __forceinline__ void build_coef(const StepParams& P, Coef& c, float rho, float rr, float rb, float ux,
                                            float uy, float uz, float vx, float vy, float vz, float pxx, float pxy,
                                            float pyy, float pyz, float pzz, float pxz) {
-    const float oms = P.oms;
+    float oms = P.oms;
+    if constexpr ((kFeat & F_FORCE) != 0)
+        if (P.tau_var) oms = 1.0f - 1.0f / tau_eff_of(P, rr, rb);
     const float usq = ux * ux + uy * uy + uz * uz;
     const float rux = rho * ux, ruy = rho * uy, ruz = rho * uz;
     const float t1 = 3.0f - 4.5f * usq;
@@ -680,10 +688,13 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             Fz = 3.0f * sz;
             const float absF = sqrtf(Fx * Fx + Fy * Fy + Fz * Fz);
             // Omega2 (collisionOperators.cuh:16-25) folded into the coefficients
-            float hA = (P.omega2_conservative && !(absF > 1.0e-4f)) ? 0.0f : 0.5f * P.A * absF;
+            float Aeff = P.A; // A_calculation (forces.cuh:114-117) at the node's relaxation time
+            if constexpr ((kFeat & F_FORCE) != 0)
+                if (P.tau_var) Aeff = P.s4 / tau_eff_of(P, nd.rr, nd.rb);
+            float hA = (P.omega2_conservative && !(absF > 1.0e-4f)) ? 0.0f : 0.5f * Aeff * absF;
             if (absF > 1.0e-4f) {
                 const float ia_ = fast_rcp(absF);
-                const float qf = 0.5f * P.A * ia_;
+                const float qf = 0.5f * Aeff * ia_;
                 // isotropic part from the same q |F|^2 as the anisotropic part, so Omega2 sums
                 // to zero over the directions in floating point too
                 hA = qf * (Fx * Fx + Fy * Fy + Fz * Fz);

@@ -66,6 +66,7 @@ class Params(ctypes.Structure):
         ("rho_scale", ctypes.c_double),
         ("u_ref", ctypes.c_double),
         ("pi_scale", ctypes.c_double),
+        ("tau_b", ctypes.c_double),
     ]
 
     @property

@@ -47,6 +47,8 @@ struct Consts {
     // constants.cuh:56-69, evaluated in R exactly as the reference's constexpr chain
     R cs2, cs4, cs6, inv_cs2, inv_cs4, inv_cs6, inv_2cs2, inv_2cs4, inv_6cs6, inv_2cs6, half;
     R taub, oms, sigma, sigma_over_4cs4, beta, rhor0, rhob0, kappa_r, kappa_b;
+    R tau_r, tau_b; // extension: phase-dependent relaxation (forces.cuh:101-108)
+    bool tau_var;
     R g[3];
     bool forced, ratio;
     // per-direction tables (stencil_ct.cuh)
@@ -70,6 +72,9 @@ struct Consts {
         taub = static_cast<R>(p.tau);
         const R omegab = static_cast<R>(1) / taub;
         oms = static_cast<R>(1) - omegab;
+        tau_var = p.tau_b > 0.0 && p.tau_b != p.tau;
+        tau_r = taub;
+        tau_b = p.tau_b > 0.0 ? static_cast<R>(p.tau_b) : taub;
         sigma = static_cast<R>(p.sigma);
         sigma_over_4cs4 = sigma / (static_cast<R>(4) * cs4);
         beta = static_cast<R>(p.beta);
@@ -280,6 +285,14 @@ struct Oracle {
         return coeff * cos_i * fieq;
     }
 
+    // extension: tau_interface (forces.cuh:101-108) with the red phase as "self"
+    R tau_eff(R rr, R rb) const {
+        const R psix = psi(rr, rb);
+        return static_cast<R>(0.5) * (static_cast<R>(1) + psix) * k.tau_r +
+               static_cast<R>(0.5) * (static_cast<R>(1) - psix) * k.tau_b;
+    }
+    R oms_of(R rr, R rb) const { return k.tau_var ? static_cast<R>(1) - static_cast<R>(1) / tau_eff(rr, rb) : k.oms; }
+
     // Bulk branch of lbm.cuh:153-208 for source node n and direction i.
     void bulk(const int *n, int i, R &fr, R &fb) const {
         const int64_t src = id3(n);
@@ -291,7 +304,7 @@ struct Oracle {
         const R ux_s = A[2][src], uy_s = A[3][src], uz_s = A[4][src];
         const R gieq = feq(i, rho_s, ux_s, uy_s, uz_s);
         const R gineqr = fneqr(i, A[5][src], A[6][src], A[7][src], A[8][src], A[9][src], A[10][src], ux_s, uy_s, uz_s);
-        const R omega1 = gieq + k.oms * gineqr;
+        const R omega1 = gieq + oms_of(rhor_s, rhob_s) * gineqr;
         const R interface_indicator = static_cast<R>(4) * rhor_s * rhob_s * inv_rhos * inv_rhos;
         R gi = omega1;
         if (k.ratio) gi += ratio_term(i, rhor_s, rhob_s);
@@ -300,7 +313,7 @@ struct Oracle {
         if (interface_indicator > static_cast<R>(1.0e-4)) {
             R Fx, Fy, Fz;
             force(n, Fx, Fy, Fz);
-            const R Acoef = k.sigma_over_4cs4 / k.taub;
+            const R Acoef = k.sigma_over_4cs4 / (k.tau_var ? tau_eff(rhor_s, rhob_s) : k.taub);
             const R absF = my_sqrt(Fx * Fx + Fy * Fy + Fz * Fz);
             if (!p.omega2_conservative || absF > static_cast<R>(1.0e-4)) gi += omega2(i, Fx, Fy, Fz, absF, Acoef);
             Deltai = recolor(i, rhor_s, rhob_s, Fx, Fy, Fz, absF);
@@ -322,7 +335,7 @@ struct Oracle {
         const R gieq = feq(i, rhoB, uxB, uyB, uzB);
         const R gineqr = fneqr(i, A[5][idF], A[6][idF], A[7][idF], A[8][idF], A[9][idF], A[10][idF], A[2][idF],
                                A[3][idF], A[4][idF]);
-        R gi = gieq + k.oms * gineqr;
+        R gi = gieq + oms_of(rrB, rbB) * gineqr;
         if (k.ratio) gi += ratio_term(i, rrB, rbB);
         if (k.forced) gi += k.half * guo(i, rhoB * k.g[0], rhoB * k.g[1], rhoB * k.g[2], uxB, uyB, uzB);
         fr = aR * gi;

@@ -85,13 +85,22 @@ CASES = {
     "rti19": lambda: mbcg.rti_params(18, 40, q=19, g=1e-4, amplitude=2.0),
     "jetz27": lambda: mbcg.jet_params(34, 30, 40, q=27, diameter=10.0, noise=0.01),
     "jetz19": lambda: mbcg.jet_params(31, 33, 26, q=19, diameter=8.0, noise=0.01),
+    "bubble27_tau2": lambda: _tau2(mbcg.bubble_params(22, q=27, radius=6.0, tau=0.7), 1.3),
+    "jetz19_tau2": lambda: _tau2(mbcg.jet_params(31, 33, 26, q=19, diameter=8.0, noise=0.01, tau=0.6), 0.9),
 }
+
+
+def _tau2(p, tau_b):
+    """phase-dependent relaxation: tau for red, tau_b for blue (forces.cuh:101-108)"""
+    p.tau_b = tau_b
+    return p
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_cases_vs_fp64_oracle(name):
     """Cases beyond the reference's reach (fully periodic bubble, walls, gravity, density
-    ratio, z jet with noise and zero-gradient outflow) against the FP64 oracle, 100 steps."""
+    ratio, z jet with noise and zero-gradient outflow, phase-dependent relaxation time) against
+    the FP64 oracle, 100 steps."""
     p = CASES[name]()
     a = ol.oracle_init(p, np.float64)
     o64 = ol.oracle_run(p, a.copy(), 100)
