@@ -23,12 +23,12 @@
 //        x: warp lanes are consecutive x nodes; neighbours exchange by __shfl_up/down_sync,
 //        y: warps are consecutive y rows; neighbours exchange through shared memory.
 // The colour gradient F (forces.cuh:20-60) is evaluated once per interface source node from a
-// 3-plane ring of psi = (rhor - rhob)/rho kept in shared memory.
+// ring of psi = (rhor - rhob)/rho planes kept in shared memory.
 //
 // Tiling.  A CTA is 32 lanes (x) x W warps (y).  Lanes 0 and 31 and warps 0 and W-1 are
 // halo sources; the CTA writes the 30 x (W-2) destination columns in between, for a chunk of
 // zchunk planes.  Each source plane arrives in shared memory through TMA
-// (cp.async.bulk.tensor.3d, one box per field, 3-slot ring tracked by mbarriers).  The ghost
+// (cp.async.bulk.tensor.3d, one box per field, 4-slot ring tracked by mbarriers).  The ghost
 // frame of a periodic x / y axis holds the periodic image of the opposite fluid layer (every
 // store writes it through), so every source a tile needs is inside its staged box
 // (bounds.cuh:34-77 wraps on read instead); the periodic images two layers out that the colour
@@ -63,7 +63,7 @@ constexpr int kTX = kStepTileX; // destination columns per CTA (30)
 constexpr int kRBX = kStepRBX;   // staged width of rhor/rhob rows (34 needed + 16-byte alignment slack)
 constexpr int kMX = kStepMX;     // staged width of the other 9 fields (32 needed + slack)
 constexpr int kPSX = 34;   // psi ring width (32 sources + 1 on each side)
-constexpr int kNSTAGE = 3; // planes staged: k, k+1 and the one in flight, k+2
+constexpr int kNSTAGE = 4; // planes staged: k, k+1, and k+2, k+3 in flight
 constexpr unsigned kFull = 0xffffffffu;
 
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
@@ -80,7 +80,7 @@ struct Geo {
     static constexpr int stage = 2 * rb_field + 9 * m_field;
     static constexpr int tx = 2 * RBY * kRBX * (int)sizeof(S) + 9 * MY * kMX * (int)sizeof(S);
     static constexpr int psi_plane = RBY * kPSX;           // floats
-    static constexpr int psi = 3 * psi_plane * 4;          // bytes
+    static constexpr int psi = kNSTAGE * psi_plane * 4;    // bytes (ring slot = stage slot)
     static constexpr int xbuf_floats = 3 * 2 * 4 * W * 32; // float4 [class][slot][row][lane]
     static constexpr int xbuf = xbuf_floats * 4;
     static constexpr int off_bar = 0;
@@ -371,7 +371,7 @@ __device__ __forceinline__ void init_stage_barriers(unsigned char* smem) {
 
 // One tile of one time step.  (bx, by, bz) index the tile in the lattice's tile grid; `step`
 // is the index of the state being written (keys the inlet noise); `phase` carries the parity
-// of the three stage mbarriers from one tile of a CTA to the next (0 before the first tile).
+// of the stage mbarriers from one tile of a CTA to the next (0 before the first tile).
 // Returns false if a staged plane never arrived (the status word is set and the CTA must stop).
 template <int Q, typename S, int W, bool kTMA, int kFeat>
 __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap* maps, int bx, int by, int bz,
@@ -583,10 +583,10 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             }
         }
         if (k + 2 <= zd1 + 1) prefetch_psi(k + 2);
-        // (2) prefetch plane k+2 into the slot plane k-1 used
-        if (k + 2 <= zd1 + 1 && k + 2 > k_issued) {
-            issue(k + 2, sl_prev);
-            k_issued = k + 2;
+        // (2) prefetch plane k+3 into the slot plane k-1 used
+        if (k + kNSTAGE - 1 <= zd1 + 1 && k + kNSTAGE - 1 > k_issued) {
+            issue(k + kNSTAGE - 1, sl_prev);
+            k_issued = k + kNSTAGE - 1;
         }
 
         // (3) this thread's source node at plane k
