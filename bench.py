@@ -135,6 +135,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ---------------------------------------------------------------- replicas (N > 1)
+def replica_time(dt: float, world: int, dist, torch, device) -> float:
+    """The slowest rank's time: every rank times its own replica between barriers, and the job
+    is done when the last one is."""
+    if world <= 1:
+        return dt
+    t = torch.tensor([dt], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_mlups(nodes: int, steps: int, dt_max: float, world: int) -> float:
+    """Whole-job MLUPS of `world` independent replicas of `nodes` fluid nodes each."""
+    return world * nodes * steps / dt_max / 1e6
+
+
 def time_device(case: mbcg.Case, steps: int, warmup: int, torch):
     """CUDA-event time of `steps` fused steps on the launching stream (state resident)."""
     stream = torch.cuda.current_stream()
@@ -390,12 +406,9 @@ def main() -> None:
             dt = time_device(case, args.steps, args.warmup, torch)
         diag = case.diagnostics()
         status = case.status()
-    if world > 1:
-        t = torch.tensor([dt], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
+    dt = replica_time(dt, world, dist, torch, "cuda")
     nodes = p.active_nodes()
-    mlups = world * nodes * args.steps / dt / 1e6
+    mlups = replica_mlups(nodes, args.steps, dt, world)
     per_launch = dt / (args.steps * launches)
     achieved = BYTES_PER_NODE[mbcg.FP32] * nodes / per_launch / 1e9
     traffic = profiled_traffic("step_kernel_jet256_fp32")
