@@ -313,16 +313,56 @@ __device__ __forceinline__ void build_coef(const StepParams& P, Coef& c, float r
 }
 
 // ------------------------------------------------------------------ accumulators
+// (rho, red) and (jx, xx) are packed pairs: they always take the same operations, which then
+// issue as one f32x2 instruction (add/fma.f32x2, sm_100 and later) instead of two.
 struct Acc {
-    float rho, jx, jy, jz, xx, xy, yy, yz, zz, xz, red;
-    __device__ __forceinline__ void zero() { rho = jx = jy = jz = xx = xy = yy = yz = zz = xz = red = 0.0f; }
+    float2 rr, jxx;
+    float jy, jz, xy, yy, yz, zz, xz;
+    __device__ __forceinline__ void zero() {
+        rr = jxx = make_float2(0.0f, 0.0f);
+        jy = jz = xy = yy = yz = zz = xz = 0.0f;
+    }
 };
+
+__device__ __forceinline__ float2 pair(float v) { return make_float2(v, v); }
+// a + f b on both halves (f = 1: a plain add, as fmaf(1, b, a) would round)
+template <int F>
+__device__ __forceinline__ float2 acc2(float2 a, float2 b) {
+    if constexpr (F == 1) return __fadd2_rn(a, b);
+    else return __ffma2_rn(pair(static_cast<float>(F)), b, a);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 r;
+    asm("{.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+// A quantity over the three x velocities of one (cy, cz): `o` = (cx = -1, cx = +1) as an f32x2
+// pair, `c` = cx = 0.  The two outer values always take the same operations.
+struct Tri {
+    float2 o;
+    float c;
+};
+__device__ __forceinline__ Tri tri(float base, float odd, float centre) {
+    return Tri{make_float2(base - odd, base + odd), centre};
+}
+__device__ __forceinline__ Tri operator+(Tri a, Tri b) { return Tri{__fadd2_rn(a.o, b.o), a.c + b.c}; }
+__device__ __forceinline__ Tri operator-(Tri a, Tri b) { return Tri{sub2(a.o, b.o), a.c - b.c}; }
+__device__ __forceinline__ Tri operator+(Tri a, float s) { return Tri{__fadd2_rn(a.o, pair(s)), a.c + s}; }
+// value at cx = i - 1
+template <int I>
+__device__ __forceinline__ float tri_at(const Tri& t) {
+    return I == 0 ? t.o.x : (I == 2 ? t.o.y : t.c);
+}
 
 // add one population of velocity (ex, ey, ez) to a destination's moment sums
 __device__ __forceinline__ void add_pop(Acc& a, float g, float r, int ex, int ey, int ez) {
-    a.rho += g;
-    a.red += r;
-    if (ex) { a.jx += ex * g; a.xx += g; }
+    a.rr.x += g;
+    a.rr.y += r;
+    if (ex) { a.jxx.x += ex * g; a.jxx.y += g; }
     if (ey) { a.jy += ey * g; a.yy += g; }
     if (ez) { a.jz += ez * g; a.zz += g; }
     if (ex && ey) a.xy += ex * ey * g;
@@ -715,20 +755,19 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             omega2_rest = hA; // rest-population part, -hA (B0 - w0) = +2/3 hA, added below in exact units
         }
         const float rho_src = active ? nd.rr + nd.rb : 0.0f;
+        // colour fractions of the x neighbours (lane -1 and lane +1) and the weighted own one
+        float2 aRlr;
+        aRlr.x = __shfl_up_sync(kFull, aR, 1);
+        aRlr.y = __shfl_down_sync(kFull, aR, 1);
 
         // separable inverse transform, x-pass: t_bc(cx) for the monomials cy^b cz^c
-        float t00[3], t10[3], t01[3], t20[3], t02[3], t11[3];
-        {
-            const float a = cf.p000 + cf.p200;
-            t00[1] = cf.p000; t00[2] = a + cf.p100; t00[0] = a - cf.p100;
-            const float b = cf.p010 + cf.p210;
-            t10[1] = cf.p010; t10[2] = b + cf.p110; t10[0] = b - cf.p110;
-            const float d = cf.p001 + cf.p201;
-            t01[1] = cf.p001; t01[2] = d + cf.p101; t01[0] = d - cf.p101;
-            t20[1] = cf.p020; t20[2] = cf.p020 + cf.p120; t20[0] = cf.p020 - cf.p120;
-            t02[1] = cf.p002; t02[2] = cf.p002 + cf.p102; t02[0] = cf.p002 - cf.p102;
-            t11[1] = cf.p011; t11[2] = cf.p011 + cf.p111; t11[0] = cf.p011 - cf.p111;
-        }
+        const Tri t00 = tri(cf.p000 + cf.p200, cf.p100, cf.p000);
+        const Tri t10 = tri(cf.p010 + cf.p210, cf.p110, cf.p010);
+        const Tri t01 = tri(cf.p001 + cf.p201, cf.p101, cf.p001);
+        const Tri t20 = tri(cf.p020, cf.p120, cf.p020);
+        const Tri t02 = tri(cf.p002, cf.p102, cf.p002);
+        const Tri t11 = tri(cf.p011, cf.p111, cf.p011);
+        const float2 rho2 = pair(rho_src);
         // Populations are carried scaled by S = 216 (D3Q27) or 36 (D3Q19), where the weights
         // are small integers that sum to S exactly: float-rounded weights do not sum to 1, and
         // that error would scale every node's mass each step (about 1.5e-8 per step for D3Q19).
@@ -758,66 +797,58 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         // y exchange.  Halo rows export one population row (cy = +1 for warp 0, -1 for warp W-1).
         auto emit = [&](auto rowsc) {
             constexpr int ROWS = decltype(rowsc)::value;
-            float s0[3][3], s1[3][3], e2[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                const float e0 = t00[i] + t20[i];
-                const float e1 = t01[i] + cf.p021;
+            // y-pass per exported row j (cy = j - 1): s0 (cz^0), s1 (cz^1), e2 (cz^0 + cz^2)
+            Tri s0[3], s1[3], e2[3];
+            {
+                const Tri e0 = t00 + t20;
+                const Tri e1 = t01 + cf.p021;
                 if (ROWS & 2) {
-                    s0[i][1] = t00[i];
-                    s1[i][1] = t01[i];
-                    e2[i][1] = t00[i] + t02[i];
+                    s0[1] = t00;
+                    s1[1] = t01;
+                    e2[1] = t00 + t02;
                 }
                 if (ROWS & 4) {
-                    s0[i][2] = e0 + t10[i];
-                    s1[i][2] = e1 + t11[i];
-                    e2[i][2] = s0[i][2] + (t02[i] + cf.p012);
+                    s0[2] = e0 + t10;
+                    s1[2] = e1 + t11;
+                    e2[2] = s0[2] + (t02 + cf.p012);
                 }
                 if (ROWS & 1) {
-                    s0[i][0] = e0 - t10[i];
-                    s1[i][0] = e1 - t11[i];
-                    e2[i][0] = s0[i][0] + (t02[i] - cf.p012);
+                    s0[0] = e0 - t10;
+                    s1[0] = e1 - t11;
+                    e2[0] = s0[0] + (t02 + (-cf.p012));
                 }
             }
             auto do_class = [&](auto czc, Acc& acc) {
                 constexpr int cz = decltype(czc)::value;
-                float g[3][3], r[3][3];
+                // populations of row j: rho + the small part (rho last, see above)
+                Tri g[3];
 #pragma unroll
-                for (int i = 0; i < 3; ++i) {
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) {
-                        const int cx = i - 1, cy = j - 1;
-                        g[i][j] = 0.0f;
-                        r[i][j] = 0.0f;
-                        if (!(ROWS & (1 << j)) || !Stencil<Q>::has(cx, cy, cz)) continue;
-                        float small =
-                            cz == 0 ? s0[i][j] : (cz > 0 ? e2[i][j] + s1[i][j] : e2[i][j] - s1[i][j]);
-                        if (cx == 0 && cy == 0 && cz == 0) small += rc0;
-                        const float vv = rho_src + small;
-                        const int sh = cx * cx + cy * cy + cz * cz;
-                        g[i][j] = kSepW ? vv : (sh == 0 ? 12.0f * vv : (sh == 1 ? vv + vv : vv));
+                for (int j = 0; j < 3; ++j) {
+                    const int cy = j - 1;
+                    g[j].o = make_float2(0.0f, 0.0f);
+                    g[j].c = 0.0f;
+                    if (!(ROWS & (1 << j))) continue;
+                    Tri small = cz == 0 ? s0[j] : (cz > 0 ? e2[j] + s1[j] : e2[j] - s1[j]);
+                    if (cy == 0 && cz == 0) small.c += rc0;
+                    const int shc = cy * cy + cz * cz; // |c|^2 of the centre; the outer ones have shc + 1
+                    if (Stencil<Q>::has(1, cy, cz)) {
+                        const float2 vv = __fadd2_rn(rho2, small.o);
+                        g[j].o = (kSepW || shc != 0) ? vv : __fadd2_rn(vv, vv);
+                    }
+                    if (Stencil<Q>::has(0, cy, cz)) {
+                        const float vv = rho_src + small.c;
+                        g[j].c = kSepW ? vv : (shc == 0 ? 12.0f * vv : (shc == 1 ? vv + vv : vv));
                     }
                 }
-                {
-                    if (any_iface) {
-#pragma unroll
-                        for (int i = 0; i < 3; ++i)
-#pragma unroll
-                            for (int j = 0; j < 3; ++j) {
-                                const int cx = i - 1, cy = j - 1, sh = cx * cx + cy * cy + cz * cz;
-                                if (!(ROWS & (1 << j))) continue;
-                                const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
-                                const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
-                                r[i][j] = sh == 0 ? aR * g[i][j] : fmaf(aR, g[i][j], dks * fc);
-                            }
-                    } else {
-#pragma unroll
-                        for (int i = 0; i < 3; ++i)
-#pragma unroll
-                            for (int j = 0; j < 3; ++j)
-                                if (ROWS & (1 << j)) r[i][j] = aR * g[i][j];
-                    }
-                }
+                // recolouring part Delta_i of the red populations (interface sources only; the
+                // red population is aR g_i + Delta_i, collisionOperators.cuh:60-80)
+                auto delta = [&](int i, int j) -> float {
+                    const int cx = i - 1, cy = j - 1, sh = cx * cx + cy * cy + cz * cz;
+                    if (!(ROWS & (1 << j)) || !Stencil<Q>::has(cx, cy, cz) || sh == 0) return 0.0f;
+                    const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
+                    const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
+                    return dks * fc;
+                };
                 if constexpr (ROWS == 7 && (kFeat & F_WALL) != 0) {
                     if (any_reflect && reflect) {
 #pragma unroll
@@ -832,38 +863,56 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                                 const float f = kSepW ? static_cast<float>((cx == 0 ? 4 : 1) * (cy == 0 ? 4 : 1) *
                                                                            (cz == 0 ? 4 : 1))
                                                       : 1.0f;
-                                add_pop(accC, f * g[i][j], f * r[i][j], -cx, -cy, -cz);
+                                const float gv = i == 0 ? g[j].o.x : (i == 2 ? g[j].o.y : g[j].c);
+                                const float rr_ = any_iface ? fmaf(aR, gv, delta(i, j)) : aR * gv;
+                                add_pop(accC, f * gv, f * rr_, -cx, -cy, -cz);
                             }
                     }
                 }
-                // x streaming: destination x receives cx=+1 from lane-1 and cx=-1 from lane+1
+                // x streaming: destination x receives cx=+1 from lane-1 and cx=-1 from lane+1.
+                // Only g crosses lanes: the destination forms each red population aR g (+ Delta)
+                // itself from the source's colour fraction (shuffled once per plane), with the
+                // very operations the source would use, so the red sums are the same bits.
                 float X0[3], X1[3], X2[3], XR[3];
+                auto xstream = [&](auto ifc) {
+                    constexpr bool kIf = decltype(ifc)::value;
 #pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    const int cy = j - 1;
-                    X0[j] = X1[j] = X2[j] = XR[j] = 0.0f;
-                    if (!(ROWS & (1 << j))) continue;
-                    if (Stencil<Q>::has(1, cy, cz)) {
-                        const float gl = __shfl_up_sync(kFull, g[2][j], 1);
-                        const float gr = __shfl_down_sync(kFull, g[0][j], 1);
-                        X2[j] = gl + gr;
-                        X0[j] = kSepW ? fmaf(4.0f, g[1][j], X2[j]) : X2[j] + g[1][j];
-                        X1[j] = gl - gr;
-                        const float rl = __shfl_up_sync(kFull, r[2][j], 1);
-                        const float rr_ = __shfl_down_sync(kFull, r[0][j], 1);
-                        XR[j] = kSepW ? fmaf(4.0f, r[1][j], rl + rr_) : (rl + rr_) + r[1][j];
-                    } else {
-                        X0[j] = g[1][j];
-                        XR[j] = r[1][j];
+                    for (int j = 0; j < 3; ++j) {
+                        const int cy = j - 1;
+                        X0[j] = X1[j] = X2[j] = XR[j] = 0.0f;
+                        if (!(ROWS & (1 << j))) continue;
+                        const float r1 = kIf ? fmaf(aR, g[j].c, delta(1, j)) : aR * g[j].c;
+                        if (Stencil<Q>::has(1, cy, cz)) {
+                            float2 glr; // (from lane - 1, from lane + 1)
+                            glr.x = __shfl_up_sync(kFull, g[j].o.y, 1);
+                            glr.y = __shfl_down_sync(kFull, g[j].o.x, 1);
+                            X2[j] = glr.x + glr.y;
+                            X0[j] = kSepW ? fmaf(4.0f, g[j].c, X2[j]) : X2[j] + g[j].c;
+                            X1[j] = glr.x - glr.y;
+                            float2 rlr;
+                            if constexpr (kIf) {
+                                float2 qlr;
+                                qlr.x = __shfl_up_sync(kFull, delta(2, j), 1);
+                                qlr.y = __shfl_down_sync(kFull, delta(0, j), 1);
+                                rlr = __ffma2_rn(aRlr, glr, qlr);
+                            } else {
+                                rlr = __fmul2_rn(aRlr, glr);
+                            }
+                            XR[j] = kSepW ? fmaf(4.0f, r1, rlr.x + rlr.y) : (rlr.x + rlr.y) + r1;
+                        } else {
+                            X0[j] = g[j].c;
+                            XR[j] = r1;
+                        }
                     }
-                }
+                };
+                if (any_iface) xstream(std::true_type{});
+                else xstream(std::false_type{});
                 if constexpr ((ROWS & 2) != 0) {
                     // cy = 0 row stays in this column: add to the destination's sums now
-                    constexpr float f = kSepW ? (cz == 0 ? 16.0f : 4.0f) : 1.0f;
-                    acc.rho = fmaf(f, X0[1], acc.rho);
-                    acc.jx = fmaf(f, X1[1], acc.jx);
-                    acc.xx = fmaf(f, X2[1], acc.xx);
-                    acc.red = fmaf(f, XR[1], acc.red);
+                    constexpr int fi = kSepW ? (cz == 0 ? 16 : 4) : 1;
+                    constexpr float f = static_cast<float>(fi);
+                    acc.rr = acc2<fi>(acc.rr, make_float2(X0[1], XR[1]));
+                    acc.jxx = acc2<fi>(acc.jxx, make_float2(X1[1], X2[1]));
                     if (cz != 0) {
                         acc.jz = fmaf(cz * f, X0[1], acc.jz);
                         acc.xz = fmaf(cz * f, X1[1], acc.xz);
@@ -873,10 +922,10 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 // cy = +1 goes to row w+1 (slot 0), cy = -1 to row w-1 (slot 1)
                 constexpr int cls = cz + 1;
                 if constexpr ((ROWS & 4) != 0) {
-                    xb_self[(cls * 2 + 0) * (W * 32)] = make_float4(X0[2], X1[2], X2[2], XR[2]);
+                    xb_self[(cls * 2 + 0) * (W * 32)] = make_float4(X0[2], XR[2], X1[2], X2[2]);
                 }
                 if constexpr ((ROWS & 1) != 0) {
-                    xb_self[(cls * 2 + 1) * (W * 32)] = make_float4(X0[0], X1[0], X2[0], XR[0]);
+                    xb_self[(cls * 2 + 1) * (W * 32)] = make_float4(X0[0], XR[0], X1[0], X2[0]);
                 }
             };
             do_class(std::integral_constant<int, -1>{}, accP);
@@ -892,26 +941,24 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         auto gather = [&](auto czc, Acc& acc) {
             constexpr int cz = decltype(czc)::value;
             constexpr int cls = cz + 1;
-            constexpr float f = (kSepW && cz == 0) ? 4.0f : 1.0f;
+            constexpr int fi = (kSepW && cz == 0) ? 4 : 1;
+            constexpr float f = static_cast<float>(fi);
             const float4 pv = xb_self[(cls * 2 + 0) * (W * 32) - 32]; // row w-1 exported cy = +1
             const float4 mv = xb_self[(cls * 2 + 1) * (W * 32) + 32]; // row w+1 exported cy = -1
-            const float P0 = pv.x, P1 = pv.y, P2 = pv.z, PR = pv.w;
-            const float M0 = mv.x, M1 = mv.y, M2 = mv.z, MR = mv.w;
-            const float s00 = P0 + M0;
-            const float s10 = P1 + M1;
-            const float d00 = P0 - M0;
-            acc.rho = fmaf(f, s00, acc.rho);
-            acc.jx = fmaf(f, s10, acc.jx);
-            acc.xx = fmaf(f, P2 + M2, acc.xx);
+            // slots (X0, XR, X1, X2)
+            const float2 s0r = __fadd2_rn(make_float2(pv.x, pv.y), make_float2(mv.x, mv.y)); // (s00, red)
+            const float2 s12 = __fadd2_rn(make_float2(pv.z, pv.w), make_float2(mv.z, mv.w)); // (s10, s20)
+            const float d00 = pv.x - mv.x;
+            acc.rr = acc2<fi>(acc.rr, s0r);
+            acc.jxx = acc2<fi>(acc.jxx, s12);
             acc.jy = fmaf(f, d00, acc.jy);
-            acc.xy = fmaf(f, P1 - M1, acc.xy);
-            acc.yy = fmaf(f, s00, acc.yy);
-            acc.red = fmaf(f, PR + MR, acc.red);
+            acc.xy = fmaf(f, pv.z - mv.z, acc.xy);
+            acc.yy = fmaf(f, s0r.x, acc.yy);
             if (cz != 0) {
-                acc.jz += cz * s00;
-                acc.xz += cz * s10;
+                acc.jz += cz * s0r.x;
+                acc.xz += cz * s12.x;
                 acc.yz += cz * d00;
-                acc.zz += s00;
+                acc.zz += s0r.x;
             }
         };
         const bool dest_row = (w >= 1 && w <= W - 2);
@@ -924,14 +971,17 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 constexpr float kS = kSepW ? 216.0f : 36.0f;
                 constexpr float sc = 1.0f / kS;
                 // correctly rounded mass quotients (no systematic bias), plain scaling for the rest
-                const float q0 = accP.rho * sc, q1 = accP.red * sc;
-                accP.rho = fmaf(fmaf(-q0, kS, accP.rho), sc, q0);
-                accP.red = fmaf(fmaf(-q1, kS, accP.red), sc, q1);
-                accP.jx *= sc; accP.jy *= sc; accP.jz *= sc;
-                accP.xx *= sc; accP.xy *= sc; accP.yy *= sc; accP.yz *= sc; accP.zz *= sc; accP.xz *= sc;
+                const float2 q = __fmul2_rn(accP.rr, pair(sc));
+                const float2 e = __ffma2_rn(make_float2(-q.x, -q.y), pair(kS), accP.rr);
+                accP.rr = __ffma2_rn(e, pair(sc), q);
+                // xx stays a scalar here: xx sc - rho/3 below then contracts to one fma, which
+                // keeps Pi's bits through the cancellation
+                accP.jxx.x *= sc; accP.jxx.y *= sc;
+                accP.jy *= sc; accP.jz *= sc;
+                accP.xy *= sc; accP.yy *= sc; accP.yz *= sc; accP.zz *= sc; accP.xz *= sc;
             }
-            const float rho = accP.rho;
-            const float rr = accP.red;
+            const float rho = accP.rr.x;
+            const float rr = accP.rr.y;
             const float rb = rho - rr;
             const float inv = fast_rcp(rho);
             float Fbx = 0.0f, Fby = 0.0f, Fbz = 0.0f;
@@ -941,12 +991,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 Fby = rho * P.g[1];
                 Fbz = rho * P.g[2];
             }
-            const float ux = (accP.jx + 0.5f * Fbx) * inv;
+            const float ux = (accP.jxx.x + 0.5f * Fbx) * inv;
             const float uy = (accP.jy + 0.5f * Fby) * inv;
             const float uz = (accP.jz + 0.5f * Fbz) * inv;
             const float ctr = cs2 * rho;
             float pi[6];
-            pi[0] = (accP.xx - ctr) - rho * ux * ux;
+            pi[0] = (accP.jxx.y - ctr) - rho * ux * ux;
             pi[1] = accP.xy - rho * ux * uy;
             pi[2] = (accP.yy - ctr) - rho * uy * uy;
             pi[3] = accP.yz - rho * uy * uz;
