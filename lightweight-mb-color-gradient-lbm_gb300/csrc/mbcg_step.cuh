@@ -114,6 +114,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 // Bounded wait: gives up after ~limit clock cycles instead of spinning forever.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, long long limit) {
+    if (mbar_try_wait(bar, parity)) return true; // the usual case: the plane is already there
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
         if (clock64() - t0 > limit) return false;
@@ -377,19 +378,20 @@ __device__ __forceinline__ float fast_rcp(float v) { return __fdividef(1.0f, v);
 // Store one node at (x, y, z); on periodic x / y axes the first and last fluid layers are also
 // written to their image in the opposite ghost layer, so the next step reads every source
 // (including wrapped ones) from the staged box (bounds.cuh:34-77 wraps on read instead).
+// ix / iy: the column's periodic image in x / y (-1: none).
 template <typename S>
 __device__ __forceinline__ void finalize_store(const StepParams& P, int x, int y, int z, float rr, float rb,
-                                               float ux, float uy, float uz, const float (&pi)[6]) {
+                                               float ux, float uy, float uz, const float (&pi)[6], int ix, int iy) {
     const float u[3] = {ux, uy, uz};
     S out[NF];
     encode<S>(P, rr, rb, u, pi, out);
     const long long zo = static_cast<long long>(z) * P.plane;
     store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + x, out);
-    const int ix = P.bc[0] == MBCG_BC_PERIODIC ? (x == 1 ? P.nx - 1 : (x == P.nx - 2 ? 0 : -1)) : -1;
-    const int iy = P.bc[1] == MBCG_BC_PERIODIC ? (y == 1 ? P.ny - 1 : (y == P.ny - 2 ? 0 : -1)) : -1;
-    if (ix >= 0) store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + ix, out);
-    if (iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + x, out);
-    if (ix >= 0 && iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + ix, out);
+    if ((ix & iy) != -1) { // either is >= 0: the faces of a periodic x / y axis only
+        if (ix >= 0) store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + ix, out);
+        if (iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + x, out);
+        if (ix >= 0 && iy >= 0) store_node<S>(P, zo + static_cast<long long>(iy) * P.pitch + ix, out);
+    }
 }
 
 // 128-byte aligned base of the dynamic shared memory (TMA destinations need it; every Geo
@@ -445,6 +447,21 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     const int ry = axis_role<kFeat>(P, 1, ys, ny);
     const bool in_xy = rx != R_OUT && ry != R_OUT;
     const int ia = P.inout_axis;
+    // the node's role, given the role of its plane
+    auto role_of = [&](int rz) -> int {
+        if (rx == R_OUT || ry == R_OUT || rz == R_OUT) return R_OUT;
+        if ((kFeat & F_WALL) && (rx == R_WALL || ry == R_WALL || rz == R_WALL)) return R_WALL;
+        if ((kFeat & F_INOUT) && (rx == R_GHOST || ry == R_GHOST || rz == R_GHOST)) return R_GHOST;
+        return R_FLUID;
+    };
+    const int role_xy = role_of(R_FLUID); // on fluid planes
+    // the inlet / outlet functors run at this column (x or y axis) or on planes 1 and nz-2 (z)
+    const bool bc_xy = (kFeat & F_INOUT) && P.do_bc && (ia == 0 || ia == 1) &&
+                       ((ia == 0 ? xs : ys) == 1 || (ia == 0 ? xs : ys) == (ia == 0 ? nx : ny) - 2);
+    const bool bc_z = (kFeat & F_INOUT) && P.do_bc && ia == 2;
+    // periodic images of this column's store (x = 1 / nx-2, y = 1 / ny-2 on a periodic axis)
+    const int img_x = P.bc[0] == MBCG_BC_PERIODIC ? (xs == 1 ? nx - 1 : (xs == nx - 2 ? 0 : -1)) : -1;
+    const int img_y = P.bc[1] == MBCG_BC_PERIODIC ? (ys == 1 ? ny - 1 : (ys == ny - 2 ? 0 : -1)) : -1;
 
     // psi fill: each thread owns <= kPsiPer ring elements; their mapping never changes along z.
     // Each element reads the staged box at the node whose stored value equals psi there (the
@@ -472,6 +489,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             psi_g[j] = static_cast<long long>(my) * P.pitch + mx;
         }
     }
+
+    // periodic images two layers out are read from global memory; most tiles have none
+    bool far_any = false;
+#pragma unroll
+    for (int j = 0; j < kPsiPer; ++j) far_any = far_any || psi_box[j] == -1;
+    far_any = __syncthreads_or(far_any) != 0;
 
     // Plane k lives in stage slot (k - kfirst) mod 3, and its psi in the ring slot of the same
     // index; the z loop advances the slot incrementally.
@@ -550,8 +573,8 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
 
     // ---- psi ring: psi = (rhor - rhob)/rho (mathUtilities.cuh:12-19) of plane k over
     // columns xb-1..xb+32 and rows yb-1..yb+W, colour-gradient neighbour rule applied
-    auto prefetch_psi = [&](int k) {
-        const long long zo = static_cast<long long>(psi_coord(P, 2, k, nz)) * P.plane;
+    auto prefetch_psi = [&](int mz) {
+        const long long zo = static_cast<long long>(mz) * P.plane;
 #pragma unroll
         for (int j = 0; j < kPsiPer; ++j)
             if (psi_box[j] == -1) {
@@ -559,10 +582,21 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 pf1[j] = Codec<S>::to_f(static_cast<const S*>(P.a[1])[zo + psi_g[j]]);
             }
     };
-    auto fill_psi = [&](int k, int sl, bool prefetched) {
+    // mz: the plane the colour-gradient rule maps k to; plane_in_box: it is the staged plane
+    auto fill_psi = [&](int mz, bool plane_in_box, int sl, bool prefetched) {
         float* ring = psi_ring + sl * G::psi_plane;
-        const int mz = psi_coord(P, 2, k, nz);
-        const bool plane_in_box = (mz == zload(k));
+        if (plane_in_box && !far_any) {
+            // every element of this tile is in the staged box (the first one of each thread
+            // always exists: the ring plane has at least 32 W elements)
+            unsigned char* st = stage_at(sl);
+            const S* r0b = rb_box(st, 0);
+            const S* r1b = rb_box(st, 1);
+            ring[tid] = psi_of<S>(P, r0b[psi_box[0]], r1b[psi_box[0]]);
+#pragma unroll
+            for (int j = 1; j < kPsiPer; ++j)
+                if (psi_box[j] >= 0) ring[tid + j * 32 * W] = psi_of<S>(P, r0b[psi_box[j]], r1b[psi_box[j]]);
+            return;
+        }
         const long long zo = static_cast<long long>(mz) * P.plane;
         unsigned char* st = stage_at(sl);
         const S* r0b = rb_box(st, 0);
@@ -596,9 +630,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             return false;
         }
     }
-    fill_psi(kfirst, 0, false);
-    fill_psi(kfirst + 1, 1, false);
-    prefetch_psi(kfirst + 2);
+    {
+        const int m0 = psi_coord(P, 2, kfirst, nz), m1 = psi_coord(P, 2, kfirst + 1, nz);
+        fill_psi(m0, m0 == zload(kfirst), 0, false);
+        fill_psi(m1, m1 == zload(kfirst + 1), 1, false);
+    }
+    if (far_any) prefetch_psi(psi_coord(P, 2, kfirst + 2, nz));
 
     Acc accP, accC, accN; // destination planes k-1, k, k+1
     accP.zero();
@@ -614,15 +651,26 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         const int sl_next = nxt(sl), sl_prev = prv(sl);
         // (1) psi of plane k+1; one barrier both publishes the ring and makes the bail decision
         // uniform (a plane that never arrived leaves garbage in the ring, which nobody reads)
+        // Plane coordinates: every mapping (staging, colour-gradient rule, node role) is the
+        // identity while planes k .. k+3 are fluid planes, which is almost every plane.
+        const bool zid = k >= 1 && k + kNSTAGE - 1 <= nz - 2;
+        int mz1 = k + 1, mz2 = k + 2, rz = R_FLUID;
+        bool inbox1 = true;
+        if (!zid) {
+            mz1 = psi_coord(P, 2, k + 1, nz);
+            inbox1 = mz1 == zload(k + 1);
+            mz2 = psi_coord(P, 2, k + 2, nz);
+            rz = axis_role<kFeat>(P, 2, k, nz);
+        }
         {
             const bool ok = wait_slot(k + 1, sl_next);
-            if (ok) fill_psi(k + 1, sl_next, true);
+            if (ok) fill_psi(mz1, inbox1, sl_next, true);
             if (__syncthreads_or(!ok)) {
                 bail(k_issued);
                 return false;
             }
         }
-        if (k + 2 <= zd1 + 1) prefetch_psi(k + 2);
+        if (far_any && k + 2 <= zd1 + 1) prefetch_psi(mz2);
         // (2) prefetch plane k+3 into the slot plane k-1 used
         if (k + kNSTAGE - 1 <= zd1 + 1 && k + kNSTAGE - 1 > k_issued) {
             issue(k + kNSTAGE - 1, sl_prev);
@@ -630,11 +678,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         }
 
         // (3) this thread's source node at plane k
-        const int rz = axis_role<kFeat>(P, 2, k, nz);
-        int role = R_FLUID;
-        if (rx == R_OUT || ry == R_OUT || rz == R_OUT) role = R_OUT;
-        else if ((kFeat & F_WALL) && (rx == R_WALL || ry == R_WALL || rz == R_WALL)) role = R_WALL;
-        else if ((kFeat & F_INOUT) && (rx == R_GHOST || ry == R_GHOST || rz == R_GHOST)) role = R_GHOST;
+        const int role = zid ? role_xy : role_of(rz);
         // Sources outside the lattice (lanes / rows past the last ghost layer) only ever stream
         // into nodes that are not destinations of this tile, so without walls every source is
         // processed branch-free; wall ghost layers hold data and must not emit.
@@ -908,15 +952,25 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 if (any_iface) xstream(std::true_type{});
                 else xstream(std::false_type{});
                 if constexpr ((ROWS & 2) != 0) {
-                    // cy = 0 row stays in this column: add to the destination's sums now
+                    // cy = 0 row stays in this column: add to the destination's sums now.  Plane
+                    // k+1 (cz = +1) receives its first contributions here: they are assigned, so
+                    // its sums need no clearing.
                     constexpr int fi = kSepW ? (cz == 0 ? 16 : 4) : 1;
                     constexpr float f = static_cast<float>(fi);
-                    acc.rr = acc2<fi>(acc.rr, make_float2(X0[1], XR[1]));
-                    acc.jxx = acc2<fi>(acc.jxx, make_float2(X1[1], X2[1]));
-                    if (cz != 0) {
-                        acc.jz = fmaf(cz * f, X0[1], acc.jz);
-                        acc.xz = fmaf(cz * f, X1[1], acc.xz);
-                        acc.zz = fmaf(f, X0[1], acc.zz);
+                    if constexpr (cz == 1) {
+                        acc.rr = fi == 1 ? make_float2(X0[1], XR[1]) : __fmul2_rn(pair(f), make_float2(X0[1], XR[1]));
+                        acc.jxx = fi == 1 ? make_float2(X1[1], X2[1]) : __fmul2_rn(pair(f), make_float2(X1[1], X2[1]));
+                        acc.jz = f * X0[1];
+                        acc.xz = f * X1[1];
+                        acc.zz = f * X0[1];
+                    } else {
+                        acc.rr = acc2<fi>(acc.rr, make_float2(X0[1], XR[1]));
+                        acc.jxx = acc2<fi>(acc.jxx, make_float2(X1[1], X2[1]));
+                        if (cz != 0) {
+                            acc.jz = fmaf(cz * f, X0[1], acc.jz);
+                            acc.xz = fmaf(cz * f, X1[1], acc.xz);
+                            acc.zz = fmaf(f, X0[1], acc.zz);
+                        }
                     }
                 }
                 // cy = +1 goes to row w+1 (slot 0), cy = -1 to row w-1 (slot 1)
@@ -951,13 +1005,21 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             const float d00 = pv.x - mv.x;
             acc.rr = acc2<fi>(acc.rr, s0r);
             acc.jxx = acc2<fi>(acc.jxx, s12);
-            acc.jy = fmaf(f, d00, acc.jy);
-            acc.xy = fmaf(f, pv.z - mv.z, acc.xy);
-            acc.yy = fmaf(f, s0r.x, acc.yy);
+            if constexpr (cz == 1) {
+                // first contributions to jy, xy, yy, yz of plane k+1 (f = 1)
+                acc.jy = d00;
+                acc.xy = pv.z - mv.z;
+                acc.yy = s0r.x;
+                acc.yz = d00;
+            } else {
+                acc.jy = fmaf(f, d00, acc.jy);
+                acc.xy = fmaf(f, pv.z - mv.z, acc.xy);
+                acc.yy = fmaf(f, s0r.x, acc.yy);
+                if (cz != 0) acc.yz += cz * d00;
+            }
             if (cz != 0) {
                 acc.jz += cz * s0r.x;
                 acc.xz += cz * s12.x;
-                acc.yz += cz * d00;
                 acc.zz += s0r.x;
             }
         };
@@ -1016,13 +1078,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 pi[2] -= Kc;
                 pi[4] -= Kc;
             }
-            finalize_store<S>(P, xs, ys, d, rr, rb, ux, uy, uz, pi);
+            finalize_store<S>(P, xs, ys, d, rr, rb, ux, uy, uz, pi, img_x, img_y);
 
-            if ((kFeat & F_INOUT) && P.do_bc && ia >= 0) {
+            if ((kFeat & F_INOUT) && (bc_xy || (bc_z && (d == 1 || d == nz - 2)))) {
                 // inlet / outlet functors fused into the first and last fluid layer
                 const int pa = ia == 0 ? xs : (ia == 1 ? ys : d);
-                const int na = ia == 0 ? nx : (ia == 1 ? ny : nz);
-                if (pa == 1 || pa == na - 2) {
+                {
                     const bool inlet = pa == 1;
                     const int gx = ia == 0 ? (inlet ? 0 : nx - 1) : xs;
                     const int gy = ia == 1 ? (inlet ? 0 : ny - 1) : ys;
@@ -1079,7 +1140,9 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                             ouz = on.uz - uc * (on.uz - uz);
                         }
                     }
-                    finalize_store<S>(P, gx, gy, gz, orr, orb, oux, ouy, ouz, pi);
+                    const int gix = P.bc[0] == MBCG_BC_PERIODIC ? (gx == 1 ? nx - 1 : (gx == nx - 2 ? 0 : -1)) : -1;
+                    const int giy = P.bc[1] == MBCG_BC_PERIODIC ? (gy == 1 ? ny - 1 : (gy == ny - 2 ? 0 : -1)) : -1;
+                    finalize_store<S>(P, gx, gy, gz, orr, orb, oux, ouy, ouz, pi, gix, giy);
                 }
             }
         }
@@ -1088,8 +1151,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             gather(std::integral_constant<int, 1>{}, accN);
         }
         accP = accC;
-        accC = accN;
-        accN.zero();
+        accC = accN; // accN is assigned before it is added to again
     }
     // every load of this tile was waited for: carry the parities over to the next tile
     phase = par;
