@@ -169,6 +169,19 @@ int64_t mbcg_steps_done(const mbcg_case *c);
 int mbcg_copy_out(mbcg_case *c, float *const host[MBCG_NFIELDS], mbcg_stream_t s);
 int mbcg_copy_in(mbcg_case *c, const float *const host[MBCG_NFIELDS], mbcg_stream_t s);
 
+/* Host-resident states through the case: for j = 0..count-1, exactly
+ *   mbcg_copy_in(c, in[j]); mbcg_step(c, nsteps); mbcg_copy_out(c, out[j]);
+ * (the same bits), with in[j] = in + j * MBCG_NFIELDS and out[j] likewise (dense FP32 arrays
+ * in the reference's layout).  The transfers of consecutive states overlap: the result of
+ * state j moves to the host while state j+1 moves in and is stepped, so the host link carries
+ * both directions at once (the host arrays should be pinned for that).  Holds four dense FP32
+ * state images on the device (two in, two out; one each where memory is short), allocated on
+ * first use and kept with the case.  Returns when out[count-1] is written;
+ * the case's state is then the last result.  (No counterpart in the reference, whose host loop
+ * copies one state out at a time: copy_out_D2H, memory.cuh:209-217.) */
+int mbcg_run_host(mbcg_case *c, int32_t count, const float *const *in, float *const *out, int32_t nsteps,
+                  mbcg_stream_t s);
+
 /* FP64 on-GPU conservation and Laplace-pressure diagnostics of state A (synchronous). */
 int mbcg_diagnostics(mbcg_case *c, mbcg_diag *out, mbcg_stream_t s);
 

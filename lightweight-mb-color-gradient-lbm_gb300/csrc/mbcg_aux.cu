@@ -390,6 +390,95 @@ __global__ void from_dense_kernel(const StepParams P, int field, const float* __
     }
 }
 
+// All 11 fields between the state and the reference's dense FP32 layout in host memory that
+// the device reads or writes directly (pinned, mapped).  blockIdx.y is the field.  Over the host
+// link a warp access costs a whole 128-byte line, so each field's element mapping is shifted to
+// start at a line boundary of its own host array (fields of the reference's dense layout are
+// not line-aligned): every warp then moves exactly one line (measured 209 / 190 GB/s read /
+// write against 160 / 136 unaligned).  The conversions are those of to_dense / from_dense.
+struct HostFields {
+    float* f[NF];
+};
+
+template <bool k32>
+__device__ __forceinline__ long long dense_to_state(const StepParams& P, long long i) {
+    if constexpr (k32) {
+        const unsigned ui = static_cast<unsigned>(i), nx = static_cast<unsigned>(P.nx), ny = static_cast<unsigned>(P.ny);
+        const unsigned r = ui / nx, x = ui - r * nx;
+        const unsigned z = r / ny, y = r - z * ny;
+        return static_cast<long long>(z) * P.plane + static_cast<long long>(y) * P.pitch + x;
+    } else {
+        const long long r = i / P.nx, x = i - r * P.nx;
+        const long long z = r / P.ny, y = r - z * P.ny;
+        return z * P.plane + y * P.pitch + x;
+    }
+}
+
+// elements of a host field before its first 128-byte line boundary
+__device__ __forceinline__ int line_shift(const float* p) {
+    return static_cast<int>(((128u - (reinterpret_cast<uintptr_t>(p) & 127u)) & 127u) >> 2);
+}
+
+template <typename S, bool k32>
+__global__ void state_to_host_kernel(const StepParams P, HostFields h, long long n) {
+    const int f = blockIdx.y;
+    float* dst = h.f[f];
+    // thread t handles element t - (32 - shift) mod 32, so element `shift` starts a warp
+    const int lead = (32 - line_shift(dst)) & 31;
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < n + lead; t += stride) {
+        const long long i = t - lead;
+        if (i < 0) continue;
+        const long long o = dense_to_state<k32>(P, i);
+        float v;
+        if constexpr (sizeof(S) == 4) {
+            v = static_cast<const float*>(P.a[f])[o];
+        } else if (f <= 1) {
+            const float s0 = Codec<S>::to_f(static_cast<const S*>(P.a[0])[o]);
+            const float c = Codec<S>::to_f(static_cast<const S*>(P.a[1])[o]);
+            const float rho = P.rho_mean + phi_of_slot(c) * P.rho_half_diff + P.rho_scale * s0;
+            float rr, rb;
+            colour_split(c, rho, rr, rb);
+            v = f == 0 ? rr : rb;
+        } else {
+            v = Codec<S>::to_f(static_cast<const S*>(P.a[f])[o]) * (f < 5 ? P.u_ref : P.pi_scale);
+        }
+        dst[i] = v;
+    }
+}
+
+template <typename S, bool k32>
+__global__ void host_to_state_kernel(const StepParams P, HostFields h, long long n) {
+    const int f = blockIdx.y;
+    if (sizeof(S) != 4 && f == 1) return; // the 16-bit forms store rhor and rhob together (f = 0)
+    const float* src = h.f[f];
+    const int lead = (32 - line_shift(src)) & 31;
+    const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+    for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < n + lead; t += stride) {
+        const long long i = t - lead;
+        if (i < 0) continue;
+        const long long o = dense_to_state<k32>(P, i);
+        if constexpr (sizeof(S) == 4) {
+            static_cast<float*>(P.b[f])[o] = src[i];
+        } else if (f == 0) {
+            const float rr = src[i], rb = h.f[1][i], rho = rr + rb;
+            if (rho == 0.0f) {
+                // unused ghost node with no fluid: zeros rather than 0/0
+                static_cast<S*>(P.b[0])[o] = Codec<S>::from_f(0.0f);
+                static_cast<S*>(P.b[1])[o] = Codec<S>::from_f(0.0f);
+            } else {
+                const S c = Codec<S>::from_f(colour_slot(rr, rb, rho));
+                const float phi = phi_of_slot(Codec<S>::to_f(c)); // the phi a reader decodes
+                static_cast<S*>(P.b[0])[o] =
+                    Codec<S>::from_f((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale);
+                static_cast<S*>(P.b[1])[o] = c;
+            }
+        } else {
+            static_cast<S*>(P.b[f])[o] = Codec<S>::from_f(src[i] * (f < 5 ? P.inv_u_ref : P.inv_pi_scale));
+        }
+    }
+}
+
 int rows_grid(const StepParams& P) {
     const long long rows = static_cast<long long>(P.ny) * P.nz;
     return static_cast<int>(std::min<long long>(rows, 65535));
@@ -544,6 +633,49 @@ cudaError_t launch_from_dense(int precision, const StepParams& P, int field, con
     case MBCG_FP16: from_dense_kernel<__half><<<rows_grid(P), 256, 0, s>>>(P, field, src, src_b); break;
     case MBCG_BF16: from_dense_kernel<__nv_bfloat16><<<rows_grid(P), 256, 0, s>>>(P, field, src, src_b); break;
     default: from_dense_kernel<float><<<rows_grid(P), 256, 0, s>>>(P, field, src, src_b); break;
+    }
+    return cudaGetLastError();
+}
+
+// grid: 4 CTAs per SM along x, one row of CTAs per field along y
+static dim3 host_grid() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return dim3(4 * (sms > 0 ? sms : 1), NF);
+}
+
+template <typename S>
+static void state_to_host_t(const StepParams& P, const HostFields& h, long long n, cudaStream_t s) {
+    if (n + 32 < (1ll << 31)) state_to_host_kernel<S, true><<<host_grid(), 256, 0, s>>>(P, h, n);
+    else state_to_host_kernel<S, false><<<host_grid(), 256, 0, s>>>(P, h, n);
+}
+template <typename S>
+static void host_to_state_t(const StepParams& P, const HostFields& h, long long n, cudaStream_t s) {
+    if (n + 32 < (1ll << 31)) host_to_state_kernel<S, true><<<host_grid(), 256, 0, s>>>(P, h, n);
+    else host_to_state_kernel<S, false><<<host_grid(), 256, 0, s>>>(P, h, n);
+}
+
+cudaError_t launch_state_to_host(int precision, const StepParams& P, float* const host[NF], cudaStream_t s) {
+    HostFields h;
+    for (int f = 0; f < NF; ++f) h.f[f] = host[f];
+    const long long n = static_cast<long long>(P.nx) * P.ny * P.nz;
+    switch (precision) {
+    case MBCG_FP16: state_to_host_t<__half>(P, h, n, s); break;
+    case MBCG_BF16: state_to_host_t<__nv_bfloat16>(P, h, n, s); break;
+    default: state_to_host_t<float>(P, h, n, s); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_host_to_state(int precision, const StepParams& P, const float* const host[NF], cudaStream_t s) {
+    HostFields h;
+    for (int f = 0; f < NF; ++f) h.f[f] = const_cast<float*>(host[f]);
+    const long long n = static_cast<long long>(P.nx) * P.ny * P.nz;
+    switch (precision) {
+    case MBCG_FP16: host_to_state_t<__half>(P, h, n, s); break;
+    case MBCG_BF16: host_to_state_t<__nv_bfloat16>(P, h, n, s); break;
+    default: host_to_state_t<float>(P, h, n, s); break;
     }
     return cudaGetLastError();
 }

@@ -256,6 +256,14 @@ struct mbcg_case {
     int w = kStepW;   // step CTA rows
     int zchunk = 16;  // destination planes per step CTA
     float* stage = nullptr; // two dense FP32 fields for host copies, allocated on first use
+    // mbcg_run_host: dense FP32 images of input and output states (two of each, or one where
+    // the device has no room for two), the two copy streams and the images' events (allocated
+    // on first use)
+    float* dense_in[2] = {nullptr, nullptr};
+    float* dense_out[2] = {nullptr, nullptr};
+    int images = 0;
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+    cudaEvent_t ev_in_ready[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {}, ev_out_free[2] = {};
 };
 
 namespace {
@@ -283,6 +291,14 @@ void free_case(mbcg_case* c) {
     if (c->diag_partials) cudaFree(c->diag_partials);
     if (c->diag_result) cudaFree(c->diag_result);
     if (c->stage) cudaFree(c->stage);
+    for (int b = 0; b < 2; ++b) {
+        if (c->dense_in[b]) cudaFree(c->dense_in[b]);
+        if (c->dense_out[b]) cudaFree(c->dense_out[b]);
+        for (cudaEvent_t e : {c->ev_in_ready[b], c->ev_in_free[b], c->ev_out_ready[b], c->ev_out_free[b]})
+            if (e) cudaEventDestroy(e);
+    }
+    if (c->s_h2d) cudaStreamDestroy(c->s_h2d);
+    if (c->s_d2h) cudaStreamDestroy(c->s_d2h);
     delete c;
 }
 
@@ -520,16 +536,39 @@ int mbcg_case_params(const mbcg_case* c, mbcg_params* out) {
     return MBCG_OK;
 }
 
-// Host copies move one whole dense field per transfer (one contiguous copy at full link
-// bandwidth: the reference's dense rows of nx floats would otherwise be copied row by row as a
-// pitched 2-D transfer) through a pair of dense device fields, converted on the device.
+// Device pointers of the host fields when every one is pinned host memory the device can
+// access directly; false for pageable memory.
+static bool host_fields_on_device(const float* const host[MBCG_NFIELDS], float* dev[MBCG_NFIELDS]) {
+    for (int i = 0; i < NF; ++i) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, host[i]) != cudaSuccess) {
+            cudaGetLastError(); // clear it: not an error of the copy
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return false;
+        dev[i] = static_cast<float*>(a.devicePointer);
+    }
+    return true;
+}
+
+// Host copies.  Pinned host fields are read or written by one kernel that also converts the
+// layout (all 11 fields, at the host link's bandwidth, no staging).  Pageable fields move one
+// whole dense field per transfer (one contiguous copy: the reference's dense rows of nx floats
+// would otherwise be copied row by row as a pitched 2-D transfer) through a pair of dense device
+// fields, converted on the device.
 int mbcg_copy_out(mbcg_case* c, float* const host[MBCG_NFIELDS], mbcg_stream_t s) {
     if (!c || !host) return fail(MBCG_E_INVALID, "null argument");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
     const mbcg_params& p = c->p;
     const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
-    if (!c->stage) MBCG_TRY(cudaMalloc(&c->stage, 2 * n * sizeof(float)), "staging allocation");
     StepParams P = make_params(c, c->cur, c->steps); // P.a = current state
+    float* dev[MBCG_NFIELDS];
+    if (host_fields_on_device(host, dev)) {
+        MBCG_TRY(launch_state_to_host(p.precision, P, dev, st), "copy out");
+        MBCG_TRY(cudaStreamSynchronize(st), "copy out");
+        return MBCG_OK;
+    }
+    if (!c->stage) MBCG_TRY(cudaMalloc(&c->stage, 2 * n * sizeof(float)), "staging allocation");
     for (int i = 0; i < NF; ++i) {
         float* buf = c->stage + (i & 1) * n; // reused two fields later, in stream order
         MBCG_TRY(launch_to_dense(p.precision, P, i, buf, st), "copy out");
@@ -544,8 +583,15 @@ int mbcg_copy_in(mbcg_case* c, const float* const host[MBCG_NFIELDS], mbcg_strea
     cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
     const mbcg_params& p = c->p;
     const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
-    if (!c->stage) MBCG_TRY(cudaMalloc(&c->stage, 2 * n * sizeof(float)), "staging allocation");
     StepParams P = make_params(c, c->cur ^ 1, c->steps); // P.b = current state
+    float* dev[MBCG_NFIELDS];
+    if (host_fields_on_device(host, dev)) {
+        MBCG_TRY(launch_host_to_state(p.precision, P, dev, st), "copy in");
+        MBCG_TRY(launch_fill_ghosts(p.precision, P, st), "ghost images");
+        MBCG_TRY(cudaStreamSynchronize(st), "copy in");
+        return MBCG_OK;
+    }
+    if (!c->stage) MBCG_TRY(cudaMalloc(&c->stage, 2 * n * sizeof(float)), "staging allocation");
     const bool pair = p.precision != MBCG_FP32; // rhor and rhob convert together
     for (int i = 0; i < NF; ++i) {
         float* buf = c->stage + (i & 1) * n;
@@ -556,6 +602,95 @@ int mbcg_copy_in(mbcg_case* c, const float* const host[MBCG_NFIELDS], mbcg_strea
     }
     MBCG_TRY(launch_fill_ghosts(p.precision, P, st), "ghost images");
     MBCG_TRY(cudaStreamSynchronize(st), "copy in");
+    return MBCG_OK;
+}
+
+// mbcg_run_host: for j = 0..count-1 the same bits as copy_in(in[j]); step(nsteps);
+// copy_out(out[j]).  Host arrays move by the copy engines between pinned host memory and dense
+// device images of the input and output states, on two streams of their own; the layout
+// conversions and the steps run on the caller's stream.  With two images each way, state j+1
+// moves in while state j is stepped and state j-1 moves out, so the host link carries both
+// directions at once and the copies never wait for a conversion.  Dependencies (events per
+// image b): an input image is refilled only after its conversion into the state (in_free[b]),
+// the conversion waits for the fill (in_ready[b]); an output image is rewritten only after its
+// copy to the host (out_free[b]), the copy waits for the conversion (out_ready[b]).
+static int host_run_images(mbcg_case* c, size_t bytes) {
+    if (c->images) return MBCG_OK;
+    MBCG_TRY(cudaStreamCreateWithFlags(&c->s_h2d, cudaStreamNonBlocking), "host-run stream");
+    MBCG_TRY(cudaStreamCreateWithFlags(&c->s_d2h, cudaStreamNonBlocking), "host-run stream");
+    for (int b = 0; b < 2; ++b)
+        for (cudaEvent_t* e : {&c->ev_in_ready[b], &c->ev_in_free[b], &c->ev_out_ready[b], &c->ev_out_free[b]})
+            MBCG_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "host-run event");
+    for (int want = 2; want >= 1; --want) {
+        bool ok = true;
+        for (int b = 0; b < want && ok; ++b)
+            ok = cudaMalloc(&c->dense_in[b], bytes) == cudaSuccess && cudaMalloc(&c->dense_out[b], bytes) == cudaSuccess;
+        if (ok) {
+            c->images = want;
+            return MBCG_OK;
+        }
+        cudaGetLastError(); // out of memory: try one image each way
+        for (int b = 0; b < 2; ++b) {
+            if (c->dense_in[b]) cudaFree(c->dense_in[b]);
+            if (c->dense_out[b]) cudaFree(c->dense_out[b]);
+            c->dense_in[b] = c->dense_out[b] = nullptr;
+        }
+    }
+    return fail(MBCG_E_NOMEM, "no device memory for the host-run images");
+}
+
+int mbcg_run_host(mbcg_case* c, int32_t count, const float* const* in, float* const* out, int32_t nsteps,
+                  mbcg_stream_t s) {
+    if (!c || (count > 0 && (!in || !out))) return fail(MBCG_E_INVALID, "null argument");
+    if (count < 0 || nsteps < 0) return fail(MBCG_E_INVALID, "negative count");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+    const mbcg_params& p = c->p;
+    const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
+    const size_t field_bytes = n * sizeof(float);
+    if (int e = host_run_images(c, NF * field_bytes)) return e;
+    // the images are free once everything the caller queued before is done
+    for (int b = 0; b < c->images; ++b) {
+        MBCG_TRY(cudaEventRecord(c->ev_in_free[b], st), "host-run event");
+        MBCG_TRY(cudaEventRecord(c->ev_out_free[b], st), "host-run event");
+    }
+    for (int j = 0; j < count; ++j) {
+        const int b = j % c->images;
+        const float* const* hin = in + static_cast<size_t>(j) * NF;
+        float* const* hout = out + static_cast<size_t>(j) * NF;
+        float* din[MBCG_NFIELDS];
+        float* dout[MBCG_NFIELDS];
+        for (int f = 0; f < NF; ++f) {
+            din[f] = c->dense_in[b] + f * n;
+            dout[f] = c->dense_out[b] + f * n;
+        }
+        // host -> input image
+        MBCG_TRY(cudaStreamWaitEvent(c->s_h2d, c->ev_in_free[b], 0), "host-run order");
+        for (int f = 0; f < NF; ++f)
+            MBCG_TRY(cudaMemcpyAsync(din[f], hin[f], field_bytes, cudaMemcpyHostToDevice, c->s_h2d), "host-run copy in");
+        MBCG_TRY(cudaEventRecord(c->ev_in_ready[b], c->s_h2d), "host-run event");
+        // input image -> state (as mbcg_copy_in), steps
+        MBCG_TRY(cudaStreamWaitEvent(st, c->ev_in_ready[b], 0), "host-run order");
+        {
+            StepParams P = make_params(c, c->cur ^ 1, c->steps); // P.b = current state
+            MBCG_TRY(launch_host_to_state(p.precision, P, din, st), "host-run copy in");
+            MBCG_TRY(launch_fill_ghosts(p.precision, P, st), "ghost images");
+        }
+        MBCG_TRY(cudaEventRecord(c->ev_in_free[b], st), "host-run event");
+        if (int e = mbcg_step(c, nsteps, s)) return e;
+        // state -> output image (as mbcg_copy_out) -> host
+        MBCG_TRY(cudaStreamWaitEvent(st, c->ev_out_free[b], 0), "host-run order");
+        {
+            StepParams P = make_params(c, c->cur, c->steps); // P.a = current state
+            MBCG_TRY(launch_state_to_host(p.precision, P, dout, st), "host-run copy out");
+        }
+        MBCG_TRY(cudaEventRecord(c->ev_out_ready[b], st), "host-run event");
+        MBCG_TRY(cudaStreamWaitEvent(c->s_d2h, c->ev_out_ready[b], 0), "host-run order");
+        for (int f = 0; f < NF; ++f)
+            MBCG_TRY(cudaMemcpyAsync(hout[f], dout[f], field_bytes, cudaMemcpyDeviceToHost, c->s_d2h), "host-run copy out");
+        MBCG_TRY(cudaEventRecord(c->ev_out_free[b], c->s_d2h), "host-run event");
+    }
+    MBCG_TRY(cudaStreamSynchronize(c->s_d2h), "host-run copy out");
+    MBCG_TRY(cudaStreamSynchronize(st), "host-run");
     return MBCG_OK;
 }
 

@@ -45,6 +45,10 @@ int diag_partials_needed(const StepParams& P);
 // one field between the state and the reference's dense FP32 layout (P.a -> dst; src -> P.b,
 // where the 16-bit forms take rhor and rhob together as field 0 and skip field 1)
 cudaError_t launch_to_dense(int precision, const StepParams& P, int field, float* dst, cudaStream_t s);
+// all fields between the state (P.a for the read, P.b for the write) and dense FP32 fields in
+// host memory the device accesses directly (device pointers of pinned host memory)
+cudaError_t launch_state_to_host(int precision, const StepParams& P, float* const host[NF], cudaStream_t s);
+cudaError_t launch_host_to_state(int precision, const StepParams& P, const float* const host[NF], cudaStream_t s);
 cudaError_t launch_from_dense(int precision, const StepParams& P, int field, const float* src, const float* src_b,
                               cudaStream_t s);
 

@@ -321,6 +321,7 @@ _PROTOS = {
     "mbcg_steps_done": (ctypes.c_int64, [_VP]),
     "mbcg_copy_out": (ctypes.c_int, [_VP, _VP * NFIELDS, _VP]),
     "mbcg_copy_in": (ctypes.c_int, [_VP, _VP * NFIELDS, _VP]),
+    "mbcg_run_host": (ctypes.c_int, [_VP, ctypes.c_int32, _P(_VP), _P(_VP), ctypes.c_int32, _VP]),
     "mbcg_diagnostics": (ctypes.c_int, [_VP, _P(Diag), _VP]),
     "mbcg_status": (ctypes.c_int, [_VP, _P(ctypes.c_int32)]),
     "mbcg_case_params": (ctypes.c_int, [_VP, _P(Params)]),
@@ -488,6 +489,27 @@ class Case:
         state = np.ascontiguousarray(state, dtype=np.float32)
         ptrs = (_VP * NFIELDS)(*[state[f].ctypes.data for f in range(NFIELDS)])
         self.lib.check(self.lib.mbcg_copy_in(self.handle, ptrs, _stream_ptr(stream)), "mbcg_copy_in")
+
+    def run_host(self, states: Sequence[np.ndarray], outs: Sequence[np.ndarray], nsteps: int = 1, stream=None):
+        """mbcg_run_host: for each j, copy_in(states[j]); step(nsteps); copy_out(outs[j]), with the
+        transfers of consecutive states overlapped (pinned host arrays, e.g. from
+        torch.empty(..., pin_memory=True).numpy(), let both link directions run at once)."""
+        if len(states) != len(outs):
+            raise ValueError("one output per input state")
+        keep = []
+        pin, pout = [], []
+        for a, o in zip(states, outs):
+            a = np.ascontiguousarray(a, dtype=np.float32)
+            if o.dtype != np.float32 or not o.flags.c_contiguous or o.shape != (NFIELDS,) + self.params.shape:
+                raise ValueError("outputs must be C-contiguous float32 arrays of the state's shape")
+            keep.append(a)
+            pin.extend(a[f].ctypes.data for f in range(NFIELDS))
+            pout.extend(o[f].ctypes.data for f in range(NFIELDS))
+        n = len(states)
+        cin = (_VP * max(1, len(pin)))(*pin)
+        cout = (_VP * max(1, len(pout)))(*pout)
+        self.lib.check(self.lib.mbcg_run_host(self.handle, n, ctypes.cast(cin, _P(_VP)), ctypes.cast(cout, _P(_VP)),
+                                              nsteps, _stream_ptr(stream)), "mbcg_run_host")
 
     def diagnostics(self, stream=None) -> dict:
         d = Diag()

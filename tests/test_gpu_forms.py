@@ -57,3 +57,73 @@ def test_storage_form_error_vs_fp64(oracle_states, prec, tol100):
     assert d["nonfinite"] == 0
     for k in ("rhor", "rhob", "u", "Pi"):
         assert e100[k] < tol100[k], (name, k, e100)
+
+
+@pytest.mark.parametrize("prec", [mbcg.FP32, mbcg.FP16, mbcg.BF16])
+def test_pinned_and_pageable_copies_agree(prec):
+    """Pinned host fields are read and written by the device directly (one kernel with the layout
+    conversion); pageable ones go through staged copies.  Both paths give the same bits, in and
+    out, on an odd-sized lattice."""
+    torch = pytest.importorskip("torch")
+    p = mbcg.jet_params(37, 29, 23, q=27, diameter=9.0, precision=prec)
+    shape = (mbcg.NFIELDS,) + p.shape
+    with mbcg.Case(p) as c:
+        c.init()
+        c.step(3)
+        pageable_out = c.copy_out()
+        pinned_out = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+        c.copy_out(out=pinned_out.numpy())
+        assert np.array_equal(pageable_out, pinned_out.numpy())
+        state = pageable_out.copy()
+    # the same state in through each path, one step, out through the pageable path
+    outs = []
+    for pinned in (False, True):
+        with mbcg.Case(p) as c:
+            if pinned:
+                src = torch.empty(shape, dtype=torch.float32, pin_memory=True)
+                src.numpy()[...] = state
+                c.copy_in(src.numpy())
+            else:
+                c.copy_in(state)
+            c.step(2)
+            outs.append(c.copy_out())
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("prec", [mbcg.FP32, mbcg.FP16])
+@pytest.mark.parametrize("nsteps", [1, 2])
+def test_run_host_matches_sequential_calls(prec, nsteps):
+    """mbcg_run_host overlaps the transfers of consecutive host states; its results are those of
+    copy_in; step; copy_out for every state, bit for bit, and the step counter advances alike."""
+    torch = pytest.importorskip("torch")
+    p = mbcg.jet_params(33, 27, 21, q=27, diameter=9.0, precision=prec)
+    shape = (mbcg.NFIELDS,) + p.shape
+    states = []
+    with mbcg.Case(p) as c:
+        c.init()
+        for _ in range(4):
+            c.step(3)
+            states.append(c.copy_out())
+    want = []
+    with mbcg.Case(p) as c:
+        for s_ in states:
+            c.copy_in(s_)
+            c.step(nsteps)
+            want.append(c.copy_out())
+        steps_seq = mbcg.Library.get().mbcg_steps_done(c.handle)
+    for pinned in (True, False):
+        if pinned:
+            ins = [torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy() for _ in states]
+            outs = [torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy() for _ in states]
+            for a, s_ in zip(ins, states):
+                a[...] = s_
+        else:
+            ins = [s_.copy() for s_ in states]
+            outs = [np.empty(shape, dtype=np.float32) for _ in states]
+        with mbcg.Case(p) as c:
+            c.run_host(ins, outs, nsteps)
+            assert mbcg.Library.get().mbcg_steps_done(c.handle) == steps_seq
+            last = c.copy_out()
+        for j in range(len(states)):
+            assert np.array_equal(outs[j], want[j]), f"state {j} (pinned={pinned})"
+        assert np.array_equal(last, want[-1])
