@@ -127,3 +127,21 @@ def test_run_host_matches_sequential_calls(prec, nsteps):
         for j in range(len(states)):
             assert np.array_equal(outs[j], want[j]), f"state {j} (pinned={pinned})"
         assert np.array_equal(last, want[-1])
+
+
+def test_run_host_edge_cases():
+    """count 0 changes nothing; nsteps 0 is copy_in + copy_out (a round trip of the state)."""
+    p = mbcg.jet_params(20, 18, 16, q=19, diameter=6.0)
+    with mbcg.Case(p) as c:
+        c.init()
+        c.step(2)
+        before = c.copy_out()
+        c.run_host([], [], 1)
+        assert np.array_equal(c.copy_out(), before)
+        assert mbcg.Library.get().mbcg_steps_done(c.handle) == 2
+        out = np.empty_like(before)
+        c.run_host([before], [out], 0)
+        assert np.array_equal(out, before)
+        assert mbcg.Library.get().mbcg_steps_done(c.handle) == 2
+        with pytest.raises(mbcg.MbcgError):
+            c.run_host([before], [out], -1)
