@@ -643,6 +643,7 @@ int mbcg_run_host(mbcg_case* c, int32_t count, const float* const* in, float* co
                   mbcg_stream_t s) {
     if (!c || (count > 0 && (!in || !out))) return fail(MBCG_E_INVALID, "null argument");
     if (count < 0 || nsteps < 0) return fail(MBCG_E_INVALID, "negative count");
+    if (count == 0) return MBCG_OK;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
     const mbcg_params& p = c->p;
     const size_t n = static_cast<size_t>(p.nx) * p.ny * p.nz;
