@@ -50,8 +50,8 @@ BYTES_PER_NODE = {mbcg.FP32: 88, mbcg.FP16: 44, mbcg.BF16: 44}
 WORKLOAD = "D3Q27 liquid jet 256x256x1024 fluid nodes (tau 0.51, sigma 1e-3, d=32 inlet, 1% noise)"
 
 
-def jet_workload(precision=mbcg.FP32, nz: int = 1024) -> mbcg.Params:
-    return mbcg.jet_params(256, 256, nz, q=27, precision=precision)
+def jet_workload(precision=mbcg.FP32, nz: int = 1024, q: int = 27) -> mbcg.Params:
+    return mbcg.jet_params(256, 256, nz, q=q, precision=precision)
 
 
 def measured_peak_hbm():
@@ -387,6 +387,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--forms", default="fp16,bf16")
     ap.add_argument("--nz", type=int, default=1024, help="fluid planes of the jet (profiling uses fewer)")
+    ap.add_argument("--q", type=int, default=27, choices=[27, 19], help="lattice of the jet (profiling the D3Q19 step)")
     ap.add_argument("--serving", default="sample", choices=["off", "sample", "full"])
     ap.add_argument("--no-configs", action="store_true", help="skip the bubble / RTI / D3Q19 lines")
     args = ap.parse_args()
@@ -406,7 +407,7 @@ def main() -> None:
     if world > 1:
         dist.init_process_group("nccl")
 
-    p = jet_workload(mbcg.FP32, args.nz)
+    p = jet_workload(mbcg.FP32, args.nz, args.q)
     peak, peak_kind = measured_peak_hbm()
     with mbcg.Case(p) as case:
         case.init()
@@ -428,7 +429,7 @@ def main() -> None:
     forms = {}
     for name in [f for f in args.forms.split(",") if f]:
         prec = {"fp16": mbcg.FP16, "bf16": mbcg.BF16}[name]
-        q = jet_workload(prec, args.nz)
+        q = jet_workload(prec, args.nz, args.q)
         with mbcg.Case(q) as c:
             c.init()
             t = time_device(c, args.steps, args.warmup, torch)
@@ -449,7 +450,7 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (analytic jet initial condition, seeded inlet noise)",
-            "config": {"workload": WORKLOAD if args.nz == 1024 else WORKLOAD.replace("x1024", f"x{args.nz}"), "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": nodes,
+            "config": {"workload": (WORKLOAD if args.nz == 1024 else WORKLOAD.replace("x1024", f"x{args.nz}")).replace("D3Q27", f"D3Q{args.q}"), "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": nodes,
                        "precision": "fp32 moments", "l2": "state 2x2.95 GB > 129 MB L2, no flush needed",
                        "parallelism": "replicas" if world > 1 else "single GPU", "zchunk": os.environ.get("MBCG_ZCHUNK", "auto")},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
