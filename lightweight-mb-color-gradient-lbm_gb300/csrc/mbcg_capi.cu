@@ -614,6 +614,13 @@ int mbcg_copy_in(mbcg_case* c, const float* const host[MBCG_NFIELDS], mbcg_strea
 // image b): an input image is refilled only after its conversion into the state (in_free[b]),
 // the conversion waits for the fill (in_ready[b]); an output image is rewritten only after its
 // copy to the host (out_free[b]), the copy waits for the conversion (out_ready[b]).
+// the 11 host fields follow one another in one array (field f at field 0 + f n)
+static bool contiguous(const float* const* h, size_t n) {
+    for (int f = 1; f < NF; ++f)
+        if (h[f] != h[0] + f * n) return false;
+    return true;
+}
+
 static int host_run_images(mbcg_case* c, size_t bytes) {
     if (c->images) return MBCG_OK;
     MBCG_TRY(cudaStreamCreateWithFlags(&c->s_h2d, cudaStreamNonBlocking), "host-run stream");
@@ -664,10 +671,13 @@ int mbcg_run_host(mbcg_case* c, int32_t count, const float* const* in, float* co
             din[f] = c->dense_in[b] + f * n;
             dout[f] = c->dense_out[b] + f * n;
         }
-        // host -> input image
+        // host -> input image (one transfer when the host fields are one contiguous array)
         MBCG_TRY(cudaStreamWaitEvent(c->s_h2d, c->ev_in_free[b], 0), "host-run order");
-        for (int f = 0; f < NF; ++f)
-            MBCG_TRY(cudaMemcpyAsync(din[f], hin[f], field_bytes, cudaMemcpyHostToDevice, c->s_h2d), "host-run copy in");
+        if (contiguous(hin, n))
+            MBCG_TRY(cudaMemcpyAsync(din[0], hin[0], NF * field_bytes, cudaMemcpyHostToDevice, c->s_h2d), "host-run copy in");
+        else
+            for (int f = 0; f < NF; ++f)
+                MBCG_TRY(cudaMemcpyAsync(din[f], hin[f], field_bytes, cudaMemcpyHostToDevice, c->s_h2d), "host-run copy in");
         MBCG_TRY(cudaEventRecord(c->ev_in_ready[b], c->s_h2d), "host-run event");
         // input image -> state (as mbcg_copy_in), steps
         MBCG_TRY(cudaStreamWaitEvent(st, c->ev_in_ready[b], 0), "host-run order");
@@ -686,8 +696,11 @@ int mbcg_run_host(mbcg_case* c, int32_t count, const float* const* in, float* co
         }
         MBCG_TRY(cudaEventRecord(c->ev_out_ready[b], st), "host-run event");
         MBCG_TRY(cudaStreamWaitEvent(c->s_d2h, c->ev_out_ready[b], 0), "host-run order");
-        for (int f = 0; f < NF; ++f)
-            MBCG_TRY(cudaMemcpyAsync(hout[f], dout[f], field_bytes, cudaMemcpyDeviceToHost, c->s_d2h), "host-run copy out");
+        if (contiguous(hout, n))
+            MBCG_TRY(cudaMemcpyAsync(hout[0], dout[0], NF * field_bytes, cudaMemcpyDeviceToHost, c->s_d2h), "host-run copy out");
+        else
+            for (int f = 0; f < NF; ++f)
+                MBCG_TRY(cudaMemcpyAsync(hout[f], dout[f], field_bytes, cudaMemcpyDeviceToHost, c->s_d2h), "host-run copy out");
         MBCG_TRY(cudaEventRecord(c->ev_out_free[b], c->s_d2h), "host-run event");
     }
     MBCG_TRY(cudaStreamSynchronize(c->s_d2h), "host-run copy out");
