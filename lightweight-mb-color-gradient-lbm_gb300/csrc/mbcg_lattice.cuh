@@ -81,17 +81,34 @@ struct Codec<float> {
     static MBCG_HD float to_f(float v) { return v; }
     static MBCG_HD float from_f(float v) { return v; }
 };
+// from_f rounds to nearest; from_f_sr rounds a pair stochastically (cvt.rs, sm_100 and later:
+// up with probability equal to the distance from the lower neighbour in ulps, drawing on 32
+// random bits; exact values, +-0 included, are unchanged).  The instruction packs a into the
+// upper half of the result and b into the lower half.
 template <>
 struct Codec<__half> {
     static constexpr int bytes = 2;
     static __device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
     static __device__ __forceinline__ __half from_f(float v) { return __float2half_rn(v); }
+    static __device__ __forceinline__ void from_f_sr(float a, float b, unsigned bits, __half& ha, __half& hb) {
+        unsigned d;
+        asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(a), "f"(b), "r"(bits));
+        ha = __ushort_as_half(static_cast<unsigned short>(d >> 16));
+        hb = __ushort_as_half(static_cast<unsigned short>(d & 0xffffU));
+    }
 };
 template <>
 struct Codec<__nv_bfloat16> {
     static constexpr int bytes = 2;
     static __device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
     static __device__ __forceinline__ __nv_bfloat16 from_f(float v) { return __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ void from_f_sr(float a, float b, unsigned bits, __nv_bfloat16& ha,
+                                                     __nv_bfloat16& hb) {
+        unsigned d;
+        asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(a), "f"(b), "r"(bits));
+        ha = __ushort_as_bfloat16(static_cast<unsigned short>(d >> 16));
+        hb = __ushort_as_bfloat16(static_cast<unsigned short>(d & 0xffffU));
+    }
 };
 
 // Colour slot of the 16-bit forms.  It holds the complement of the colour field,
@@ -167,6 +184,22 @@ MBCG_HD int features_of(const StepParams& P) {
     if (P.forced || P.ratio || P.tau_var) f |= F_FORCE;
     if (P.inout_axis >= 0) f |= F_INOUT;
     return f;
+}
+
+// Random bits for the stochastic rounding of the 16-bit forms: Chris Wellons' "lowbias32"
+// integer hash (public domain, github.com/skeeto/hash-prospector), keyed by (seed, step, node,
+// slot pair), so a run is reproducible and a restart continues bit for bit.
+MBCG_HD unsigned lowbias32(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+// per (seed, step): the base every node's key is offset from
+MBCG_HD unsigned round_key_base(unsigned long long seed, long long step) {
+    return lowbias32(static_cast<unsigned>(step) ^ lowbias32(static_cast<unsigned>(seed) + 0x632BE5ABU));
 }
 
 // Counter-based inlet-noise generator: SplitMix64 finaliser (Steele, Lea & Flood 2014) on

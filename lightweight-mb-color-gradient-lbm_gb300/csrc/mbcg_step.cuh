@@ -197,20 +197,34 @@ __device__ __forceinline__ void decode(const StepParams& P, const float (&v)[NF]
     }
 }
 
+// The 16-bit forms round every stored slot stochastically (`key`: the node's random stream).
+// Rounded to nearest, a slowly changing state is rounded the same way step after step and the
+// errors add up (field error growing in proportion to the step count); rounded stochastically
+// they are unbiased and independent from step to step.
 template <typename S>
 __device__ __forceinline__ void encode(const StepParams& P, float rr, float rb, const float (&u)[3],
-                                       const float (&pi)[6], S (&out)[NF]) {
+                                       const float (&pi)[6], S (&out)[NF], unsigned key) {
     if constexpr (sizeof(S) == 4) {
+        (void)key;
         out[0] = rr; out[1] = rb; out[2] = u[0]; out[3] = u[1]; out[4] = u[2];
         for (int i = 0; i < 6; ++i) out[5 + i] = pi[i];
     } else {
         const float rho = rr + rb;
-        out[1] = Codec<S>::from_f(colour_slot(rr, rb, rho));
+        S unused;
+        Codec<S>::from_f_sr(colour_slot(rr, rb, rho), 0.0f, lowbias32(key), out[1], unused);
         const float phi = phi_of_slot(Codec<S>::to_f(out[1])); // the phi a reader decodes
-        out[0] = Codec<S>::from_f((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale);
-        for (int i = 0; i < 3; ++i) out[2 + i] = Codec<S>::from_f(u[i] * P.inv_u_ref);
-        for (int i = 0; i < 6; ++i) out[5 + i] = Codec<S>::from_f(pi[i] * P.inv_pi_scale);
+        Codec<S>::from_f_sr((rho - (P.rho_mean + phi * P.rho_half_diff)) * P.inv_rho_scale, u[0] * P.inv_u_ref,
+                            lowbias32(key + 1), out[0], out[2]);
+        Codec<S>::from_f_sr(u[1] * P.inv_u_ref, u[2] * P.inv_u_ref, lowbias32(key + 2), out[3], out[4]);
+        Codec<S>::from_f_sr(pi[0] * P.inv_pi_scale, pi[1] * P.inv_pi_scale, lowbias32(key + 3), out[5], out[6]);
+        Codec<S>::from_f_sr(pi[2] * P.inv_pi_scale, pi[3] * P.inv_pi_scale, lowbias32(key + 4), out[7], out[8]);
+        Codec<S>::from_f_sr(pi[4] * P.inv_pi_scale, pi[5] * P.inv_pi_scale, lowbias32(key + 5), out[9], out[10]);
     }
+}
+
+// random stream of node (x, y, z) given the step's key base: six consecutive keys per node
+__device__ __forceinline__ unsigned node_round_key(const StepParams& P, unsigned base, int x, int y, int z) {
+    return base + 6U * static_cast<unsigned>((z * P.ny + y) * P.nx + x);
 }
 
 template <typename S>
@@ -381,10 +395,11 @@ __device__ __forceinline__ float fast_rcp(float v) { return __fdividef(1.0f, v);
 // ix / iy: the column's periodic image in x / y (-1: none).
 template <typename S>
 __device__ __forceinline__ void finalize_store(const StepParams& P, int x, int y, int z, float rr, float rb,
-                                               float ux, float uy, float uz, const float (&pi)[6], int ix, int iy) {
+                                               float ux, float uy, float uz, const float (&pi)[6], int ix, int iy,
+                                               unsigned key_base) {
     const float u[3] = {ux, uy, uz};
     S out[NF];
-    encode<S>(P, rr, rb, u, pi, out);
+    encode<S>(P, rr, rb, u, pi, out, sizeof(S) == 4 ? 0U : node_round_key(P, key_base, x, y, z));
     const long long zo = static_cast<long long>(z) * P.plane;
     store_node<S>(P, zo + static_cast<long long>(y) * P.pitch + x, out);
     if ((ix & iy) != -1) { // either is >= 0: the faces of a periodic x / y axis only
@@ -455,6 +470,8 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         return R_FLUID;
     };
     const int role_xy = role_of(R_FLUID); // on fluid planes
+    // stochastic rounding of the 16-bit stores: key base of this step
+    const unsigned key_base = sizeof(S) == 4 ? 0U : round_key_base(P.seed, step);
     // the inlet / outlet functors run at this column (x or y axis) or on planes 1 and nz-2 (z)
     const bool bc_xy = (kFeat & F_INOUT) && P.do_bc && (ia == 0 || ia == 1) &&
                        ((ia == 0 ? xs : ys) == 1 || (ia == 0 ? xs : ys) == (ia == 0 ? nx : ny) - 2);
@@ -1078,7 +1095,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 pi[2] -= Kc;
                 pi[4] -= Kc;
             }
-            finalize_store<S>(P, xs, ys, d, rr, rb, ux, uy, uz, pi, img_x, img_y);
+            finalize_store<S>(P, xs, ys, d, rr, rb, ux, uy, uz, pi, img_x, img_y, key_base);
 
             if ((kFeat & F_INOUT) && (bc_xy || (bc_z && (d == 1 || d == nz - 2)))) {
                 // inlet / outlet functors fused into the first and last fluid layer
@@ -1142,7 +1159,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                     }
                     const int gix = P.bc[0] == MBCG_BC_PERIODIC ? (gx == 1 ? nx - 1 : (gx == nx - 2 ? 0 : -1)) : -1;
                     const int giy = P.bc[1] == MBCG_BC_PERIODIC ? (gy == 1 ? ny - 1 : (gy == ny - 2 ? 0 : -1)) : -1;
-                    finalize_store<S>(P, gx, gy, gz, orr, orb, oux, ouy, ouz, pi, gix, giy);
+                    finalize_store<S>(P, gx, gy, gz, orr, orb, oux, ouy, ouz, pi, gix, giy, key_base);
                 }
             }
         }
