@@ -1,5 +1,7 @@
 """FP16 / BF16 moment storage (scaled deviations, FP32 arithmetic) against the FP64 oracle on a
 reduced jet with the jet configuration's physics (tau 0.51, sigma 1e-3, 1% inlet noise)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -177,3 +179,26 @@ def test_run_host_edge_cases():
         assert mbcg.Library.get().mbcg_steps_done(c.handle) == 2
         with pytest.raises(mbcg.MbcgError):
             c.run_host([before], [out], -1)
+
+
+@pytest.mark.skipif(not os.environ.get("MBCG_LONG"), reason="10^4-step FP64 oracle run (~6 min of host CPU): set MBCG_LONG=1")
+def test_forms_error_at_10k_steps():
+    """Field error against the FP64 oracle after 10^4 steps (the jet above): FP32 stays at its
+    100-step level; the 16-bit forms, stochastically rounded, grow like a random walk (measured
+    FP32 2.2e-5, 1.4e-5, 1.1e-5, 1.7e-4; FP16 3.1e-2, 1.9e-2, 3.9e-3, 5.4e-2; BF16 0.22, 0.14,
+    2.5e-2, 0.42)."""
+    p = jet(mbcg.FP32)
+    a = ol.oracle_init(p, np.float64)
+    ref = ol.oracle_run(p, a.copy(), 10000)
+    idx = written_nodes(p)
+    bounds = {mbcg.FP32: {"rhor": 5e-5, "rhob": 5e-5, "u": 3e-5, "Pi": 5e-4},
+              mbcg.FP16: {"rhor": 6e-2, "rhob": 4e-2, "u": 1e-2, "Pi": 0.1},
+              mbcg.BF16: {"rhor": 0.45, "rhob": 0.3, "u": 6e-2, "Pi": 0.8}}
+    for prec, tol in bounds.items():
+        with mbcg.Case(jet(prec)) as c:
+            c.copy_in(a.astype(np.float32))
+            c.step(10000)
+            e = group_errors(c.copy_out(), ref, idx)
+        print(f"\n{prec}: step 10000 {e}")
+        for k, v in tol.items():
+            assert e[k] < v, (prec, k, e)
