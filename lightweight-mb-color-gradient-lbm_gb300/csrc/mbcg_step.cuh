@@ -1221,6 +1221,7 @@ cudaError_t launch_w(bool tma, const StepParams& P, const TensorMaps& T, cudaStr
     const int f = features_of(P);
     if (f == 0) return launch_one<Q, S, W, true, 0>(P, T, s);
     if (f == F_INOUT) return launch_one<Q, S, W, true, F_INOUT>(P, T, s);
+    if ((f & F_INOUT) == 0) return launch_one<Q, S, W, true, F_WALL | F_FORCE>(P, T, s); // walls, force
     return launch_one<Q, S, W, true, F_ALL>(P, T, s);
 }
 
