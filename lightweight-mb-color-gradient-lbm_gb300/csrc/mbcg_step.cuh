@@ -224,7 +224,11 @@ __device__ __forceinline__ void encode(const StepParams& P, float rr, float rb, 
 
 // random stream of node (x, y, z) given the step's key base: six consecutive keys per node
 __device__ __forceinline__ unsigned node_round_key(const StepParams& P, unsigned base, int x, int y, int z) {
-    return base + 6U * static_cast<unsigned>((z * P.ny + y) * P.nx + x);
+    // unsigned arithmetic: the index wraps (harmlessly) on lattices beyond 2^32 nodes
+    const unsigned node = (static_cast<unsigned>(z) * static_cast<unsigned>(P.ny) + static_cast<unsigned>(y)) *
+                              static_cast<unsigned>(P.nx) +
+                          static_cast<unsigned>(x);
+    return base + 6U * node;
 }
 
 template <typename S>
