@@ -665,7 +665,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
 
     constexpr float w0 = Stencil<Q>::wk(0);
     constexpr float cs2 = 1.0f / 3.0f;
-    float4* xb_self = xbuf + w * 32 + lane; // (X0, X1, X2, XR) of one exported row
+    float4* xb_self = xbuf + w * 32 + lane; // (X0, XR, X1, X2) of one exported row
 
     int sl = 1; // slot of plane k (k starts at kfirst + 1)
     for (int k = zd0 - 1; k <= zd1; ++k, sl = nxt(sl)) {
@@ -820,7 +820,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             omega2_rest = hA; // rest-population part, -hA (B0 - w0) = +2/3 hA, added below in exact units
         }
         const float rho_src = active ? nd.rr + nd.rb : 0.0f;
-        // colour fractions of the x neighbours (lane -1 and lane +1) and the weighted own one
+        // colour fractions of the x neighbours (lane -1 and lane +1)
         float2 aRlr;
         aRlr.x = __shfl_up_sync(kFull, aR, 1);
         aRlr.y = __shfl_down_sync(kFull, aR, 1);
