@@ -307,7 +307,7 @@ typedef struct mbcg_server mbcg_server;
 
 typedef struct mbcg_server_config {
     int64_t arena_bytes;    /* device memory for resident states (0: 70% of the free memory)  */
-    int32_t max_live;       /* lattices resident at once (0: 64; at most 4096)                 */
+    int32_t max_live;       /* lattices resident at once (0: 64; at most 64)                   */
     int32_t chunk_steps;    /* launches per graph replay, the admission granularity (0: 16)    */
     int32_t keep_results;   /* 1: finished states stay resident until fetched or released      */
     int32_t backfill;       /* 1: admit later requests that fit while an earlier one waits     */

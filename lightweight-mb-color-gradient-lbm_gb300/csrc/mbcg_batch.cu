@@ -14,20 +14,19 @@ namespace mbcg {
 
 namespace {
 
+__constant__ StepParams c_batch_params[kBatchParamSlots * 2]; // [slot][parity]
+
 template <int W>
 __global__ void __launch_bounds__(32 * W, 1)
     batch_kernel(const BatchCase* __restrict__ cases, const BatchTile* __restrict__ tiles, int ntiles,
                  const ChunkState* __restrict__ chunk, int* __restrict__ counters, int j) {
-    __shared__ __align__(16) StepParams sP;
     __shared__ int s_tile;
     unsigned char* smem = aligned_smem_base();
     init_stage_barriers(smem);
     uint32_t phase = 0;
     const int tid = threadIdx.y * 32 + threadIdx.x;
-    constexpr int kWords = static_cast<int>(sizeof(StepParams) / sizeof(int));
-    static_assert(sizeof(StepParams) % sizeof(int) == 0, "StepParams is copied as words");
     for (;;) {
-        __syncthreads(); // everyone is done with the previous tile's s_tile and sP
+        __syncthreads(); // everyone is done with the previous tile's s_tile
         if (tid == 0) s_tile = atomicAdd(&counters[j], 1);
         __syncthreads();
         const int t = s_tile;
@@ -37,12 +36,7 @@ __global__ void __launch_bounds__(32 * W, 1)
         if (j >= cs.nsteps) continue;
         const int par = cs.parity0 ^ (j & 1);
         const BatchCase& C = cases[bt.slot];
-        {
-            const int* src = reinterpret_cast<const int*>(&C.P[par]);
-            int* dst = reinterpret_cast<int*>(&sP);
-            for (int i = tid; i < kWords; i += 32 * W) dst[i] = src[i];
-        }
-        __syncthreads();
+        const StepParams& sP = c_batch_params[bt.slot * 2 + par];
         const CUtensorMap* maps = C.maps[par];
         const long long step = cs.step0 + j + 1;
         bool ok = true;
@@ -91,6 +85,11 @@ __global__ void state_hash_kernel(const StepParams P, unsigned long long* out) {
 } // namespace
 
 int batch_smem_bytes() { return Geo<float, kBatchW>::smem; }
+
+cudaError_t upload_batch_params(const StepParams* params, int n, cudaStream_t s) {
+    if (n < 0 || n > kBatchParamSlots) return cudaErrorInvalidValue;
+    return cudaMemcpyToSymbolAsync(c_batch_params, params, sizeof(StepParams) * 2 * n, 0, cudaMemcpyHostToDevice, s);
+}
 
 cudaError_t launch_batch(const BatchCase* cases, const BatchTile* tiles, int ntiles, const ChunkState* chunk,
                          int* counters, int j, int grid, cudaStream_t s) {

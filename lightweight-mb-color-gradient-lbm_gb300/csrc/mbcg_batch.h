@@ -43,6 +43,13 @@ struct ChunkState {
 };
 
 constexpr int kBatchW = kStepW; // rows of the batch kernel's CTAs
+// Lattices resident at once: the batch kernel reads each one's step parameters (both parities)
+// from a constant-memory table of this many slots (2 x 64 x 392 bytes), as uniform loads the
+// instructions take as operands, where a copy in shared memory costs a load into a register per use.
+constexpr int kBatchParamSlots = 64;
+// Copies n slots' parameters (StepParams[n][2], host memory valid until the copy has executed)
+// into that table, in stream order.
+cudaError_t upload_batch_params(const StepParams* params, int n, cudaStream_t s);
 
 cudaError_t launch_batch(const BatchCase* cases, const BatchTile* tiles, int ntiles, const ChunkState* chunk,
                          int* counters, int j, int grid, cudaStream_t s);

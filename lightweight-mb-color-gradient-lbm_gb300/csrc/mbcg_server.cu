@@ -40,7 +40,7 @@ using namespace mbcg;
 namespace {
 
 constexpr int kRing = 4;         // pinned staging buffers per kind of upload
-constexpr int kMaxLiveCap = 4096; // slot index fits the 16-bit tile field
+constexpr int kMaxLiveCap = kBatchParamSlots; // slots of the batch kernel's parameter table
 constexpr size_t kAlign = 256;
 
 int fail(int code, const std::string& msg) {
@@ -269,6 +269,23 @@ cudaError_t upload(mbcg_server* s, Staging* ring, int* idx, void* dst, const voi
     return e;
 }
 
+// the slots' step parameters into the batch kernel's constant table, through the same staging ring
+cudaError_t upload_params(mbcg_server* s) {
+    const int n = s->cfg.max_live;
+    Staging* b = nullptr;
+    cudaError_t e = stage(s->case_stage, &s->case_ring, sizeof(StepParams) * 2 * n, &b);
+    if (e != cudaSuccess) return e;
+    StepParams* h = static_cast<StepParams*>(b->host);
+    for (int slot = 0; slot < n; ++slot) {
+        h[2 * slot] = s->h_cases[slot].P[0];
+        h[2 * slot + 1] = s->h_cases[slot].P[1];
+    }
+    e = upload_batch_params(h, n, s->st);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev, s->st);
+    if (e == cudaSuccess) b->pending = true;
+    return e;
+}
+
 int live_count(const mbcg_server* s) {
     int n = 0;
     for (int64_t id : s->slot_req) n += id != 0;
@@ -471,6 +488,7 @@ cudaError_t rebuild(mbcg_server* s) {
     }
     cudaError_t e = upload(s, s->case_stage, &s->case_ring, s->d_cases, s->h_cases,
                            sizeof(BatchCase) * s->cfg.max_live);
+    if (e == cudaSuccess) e = upload_params(s);
     if (e != cudaSuccess) return e;
     std::vector<BatchTile> tiles(best_items.size());
     for (size_t i = 0; i < best_items.size(); ++i) tiles[i] = best_items[i].t;
@@ -779,6 +797,7 @@ int calibrate(mbcg_server* s) {
             BatchCase& C = s->h_cases[0];
             C.P[0].zchunk = C.P[1].zchunk = depth;
             e = cudaMemcpyAsync(s->d_cases, &C, sizeof(C), cudaMemcpyHostToDevice, s->st);
+            if (e == cudaSuccess) e = upload_batch_params(C.P, 1, s->st); // pageable: staged before return
             std::vector<BatchTile> tiles;
             for (int bz = 0; bz < 128 / depth; ++bz)
                 for (int by = 0; by < gy; ++by)
@@ -889,7 +908,7 @@ int mbcg_server_create(const mbcg_server_config* cfg_in, mbcg_server** out) {
     if (cfg_in) cfg = *cfg_in;
     else mbcg_server_config_default(&cfg);
     if (cfg.max_live <= 0) cfg.max_live = 64;
-    if (cfg.max_live > kMaxLiveCap) return fail(MBCG_E_INVALID, "max_live above 4096");
+    if (cfg.max_live > kMaxLiveCap) return fail(MBCG_E_INVALID, "max_live above 64");
     if (cfg.chunk_steps <= 0) cfg.chunk_steps = 16;
     if (cfg.chunk_steps > 1024) return fail(MBCG_E_INVALID, "chunk_steps above 1024");
     if (cfg.zchunk < 0) return fail(MBCG_E_INVALID, "negative zchunk");
