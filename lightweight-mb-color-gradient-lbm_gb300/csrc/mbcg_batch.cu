@@ -3,9 +3,9 @@
 //
 // The work is a flat queue of tiles (BatchTile) over all live lattices, sorted by the host
 // (largest tiles first, grouped by body).  Each CTA of a grid of at most one CTA per SM takes
-// the next tile with an atomic counter, copies that lattice's step parameters into shared
-// memory and runs the same step_tile() as the plain kernel, instantiated for the lattice's
-// (Q, storage, feature set).  The stage mbarriers are initialised once per CTA; their phase
+// the next tile with an atomic counter and runs the same step_tile() as the plain kernel,
+// instantiated for the lattice's (Q, storage, feature set), on that lattice's step parameters in
+// a constant-memory table indexed by slot.  The stage mbarriers are initialised once per CTA; their phase
 // carries from tile to tile.
 #include "mbcg_batch.h"
 #include "mbcg_step.cuh"
@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(32 * W, 1)
         if (j >= cs.nsteps) continue;
         const int par = cs.parity0 ^ (j & 1);
         const BatchCase& C = cases[bt.slot];
-        const StepParams& sP = c_batch_params[bt.slot * 2 + par];
+        const StepParams& sP = c_batch_params[bt.slot * 2 + par]; // this lattice, this parity
         const CUtensorMap* maps = C.maps[par];
         const long long step = cs.step0 + j + 1;
         bool ok = true;
