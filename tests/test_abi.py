@@ -80,3 +80,21 @@ def test_noise_generator_is_uniform_and_seeded():
     assert abs(sum(xs) / len(xs)) < 0.05
     assert ol.oracle_noise(12345, 7, 11, 0) == ol.oracle_noise(12345, 7, 11, 0)
     assert ol.oracle_noise(12345, 7, 11, 0) != ol.oracle_noise(12345, 8, 11, 0)
+
+
+@pytest.mark.parametrize("field,value", [("max_live", 65), ("chunk_steps", 2000), ("zchunk", -1), ("policy", 7)])
+def test_server_config_is_validated_before_any_device_work(field, value):
+    """mbcg_server_create rejects a configuration outside its limits (at most 64 live lattices:
+    the batch kernel's constant parameter table) with MBCG_E_INVALID, before touching a GPU."""
+    lib = mbcg.Library.get()
+    cfg = mbcg.ServerConfig()
+    lib.mbcg_server_config_default(ctypes.byref(cfg))
+    setattr(cfg, field, value)
+    h = ctypes.c_void_p()
+    assert lib.mbcg_server_create(ctypes.byref(cfg), ctypes.byref(h)) == -1  # MBCG_E_INVALID
+    assert not h.value
+
+
+def test_run_host_rejects_a_null_case():
+    lib = mbcg.Library.get()
+    assert lib.mbcg_run_host(None, 0, None, None, 1, None) == -1  # MBCG_E_INVALID
