@@ -371,11 +371,6 @@ __device__ __forceinline__ Tri tri(float base, float odd, float centre) {
 __device__ __forceinline__ Tri operator+(Tri a, Tri b) { return Tri{__fadd2_rn(a.o, b.o), a.c + b.c}; }
 __device__ __forceinline__ Tri operator-(Tri a, Tri b) { return Tri{sub2(a.o, b.o), a.c - b.c}; }
 __device__ __forceinline__ Tri operator+(Tri a, float s) { return Tri{__fadd2_rn(a.o, pair(s)), a.c + s}; }
-// value at cx = i - 1
-template <int I>
-__device__ __forceinline__ float tri_at(const Tri& t) {
-    return I == 0 ? t.o.x : (I == 2 ? t.o.y : t.c);
-}
 
 // add one population of velocity (ex, ey, ez) to a destination's moment sums
 __device__ __forceinline__ void add_pop(Acc& a, float g, float r, int ex, int ey, int ez) {
@@ -663,7 +658,6 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     accC.zero();
     accN.zero();
 
-    constexpr float w0 = Stencil<Q>::wk(0);
     constexpr float cs2 = 1.0f / 3.0f;
     float4* xb_self = xbuf + w * 32 + lane; // (X0, XR, X1, X2) of one exported row
 
