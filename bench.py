@@ -227,6 +227,48 @@ def cpu_leg(budget_s: float, threads: int, real_bytes: int = 4) -> dict:
                                       f"{'FP32' if real_bytes == 4 else 'FP64'} oracle, {dt:.1f} s"}
 
 
+def reference_cuda_leg(steps: int, warmup: int, torch) -> dict:
+    """The reference's own CUDA build on the same GB300: its unmodified RCSKernel +
+    JetBoundaryConditions (kernels.cu:102-131, compiled for sm_103a with the jet's constants by
+    oracle/Makefile `cubin`, block 32x4x2 as compile.sh:34-36) on the jet with the same fluid-node
+    count (256 x 1024 x 256, the jet along the reference's y axis), timed with CUDA events on the
+    launching stream over the same steps and warm-up.  A reported baseline, never the product."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from ref_cuda import RefKernels, cubin_path
+    path = cubin_path("jet256")
+    if not os.path.exists(path):
+        print(f"bench.py: reference CUDA cubin {path} missing (build it with __graft_entry__.build() where "
+              f"the reference sources are mounted)", file=sys.stderr)
+        return {"unavailable": f"reference cubin {os.path.relpath(path, ROOT)} missing"}
+    NX, NY, NZ = 258, 1026, 258
+    k = RefKernels(path, (NX, NY, NZ))
+    p = mbcg.reference_jet_params(NX, NY, NZ, q=27, tau=0.51, sigma=1e-3, beta=0.7, radius=16.0)
+    lib = mbcg.Library.get()
+    a = [torch.zeros(NX * NY * NZ, device="cuda") for _ in range(11)]
+    m = mbcg.moments_from_tensors(a, NX)
+    lib.check(lib.mbcg_init_moments(ctypes.byref(p), ctypes.byref(m), None), "init")
+    b = [t.clone() for t in a]
+    for _ in range(warmup):
+        k.step(a, b)
+        a, b = b, a
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        k.step(a, b)
+        a, b = b, a
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / steps
+    nodes = (NX - 2) * (NY - 2) * (NZ - 2)
+    del a, b
+    torch.cuda.empty_cache()
+    return {"value": nodes / ms / 1e3, "unit": "MLUPS", "ms_per_step": ms, "steps": steps, "warmup": warmup,
+            "what": "reference kernels.cu (RCSKernel + JetBoundaryConditions), unmodified, sm_103a cubin, "
+                    "D3Q27 jet 256x1024x256 fluid nodes (jet along y), block 32x4x2",
+            "roofline_frac": BYTES_PER_NODE[mbcg.FP32] * nodes / (ms * 1e-3) / 1e9 / measured_peak_hbm()[0]}
+
+
 # ---------------------------------------------------------------- serving workload
 # ---------------------------------------------------------------- the other configurations
 def configs_leg(torch) -> dict:
@@ -306,15 +348,21 @@ def serve_batched(reqs, policy=mbcg.POLICY_FIFO) -> dict:
 
 def serve_sequential(reqs, torch) -> dict:
     t0 = time.perf_counter()
-    ttc, done, mass = [], [], []
+    ttc, done, mass, dev = [], [], [], []
+    stream = torch.cuda.current_stream()
     for r in reqs:
         now = time.perf_counter() - t0
         if now < r["t"]:
             time.sleep(r["t"] - now)
         with mbcg.Case(r["p"]) as c:
             c.init()
-            c.step(r["steps"])
-            d = c.diagnostics()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            c.step(r["steps"], stream)
+            e.record(stream)
+            d = c.diagnostics(stream)
+            e.synchronize()
+            dev.append(s.elapsed_time(e) / 1e3)
         fin = time.perf_counter() - t0
         done.append(fin)
         ttc.append(fin - r["t"])
@@ -322,7 +370,25 @@ def serve_sequential(reqs, torch) -> dict:
     span = max(done) - reqs[0]["t"]
     work = sum(r["p"].active_nodes() * r["steps"] for r in reqs)
     return {"cases_per_s": len(reqs) / span, "p50_s": _pct(ttc, 50), "p99_s": _pct(ttc, 99), "makespan_s": span,
-            "mlups": work / span / 1e6, "mass": mass}
+            "mlups": work / span / 1e6, "mass": mass, "device_s": dev}
+
+
+def serving_bound(reqs, device_s) -> dict:
+    """Ceiling on cases/s for this request stream when every request runs at the plain kernel's
+    rate on its own lattice (its measured single-case stepping time) with no other cost: the
+    makespan of the best preemptive one-at-a-time schedule with these release times,
+    max over k of (a_k + the work released at or after a_k) - a_0."""
+    order = sorted(range(len(reqs)), key=lambda i: reqs[i]["t"])
+    a = [reqs[i]["t"] for i in order]
+    t = [device_s[i] for i in order]
+    tail, best = 0.0, 0.0
+    for k in range(len(a) - 1, -1, -1):
+        tail += t[k]
+        best = max(best, a[k] + tail)
+    span = best - a[0]
+    return {"cases_per_s": len(reqs) / span, "makespan_s": span, "device_s_total": sum(t),
+            "how": "release times of the stream, per-request device time of the plain step kernel alone "
+                   "(CUDA events around its steps in the sequential run), no set-up, admission or host cost"}
 
 
 def serving_leg(mode: str, torch) -> dict:
@@ -335,6 +401,7 @@ def serving_leg(mode: str, torch) -> dict:
     bs = serve_batched(reqs, mbcg.POLICY_SJF)
     bs.pop("mass")
     s = serve_sequential(reqs, torch)
+    bound = serving_bound(reqs, s.pop("device_s"))
     rel = 0.0
     for (br, bb), (sr, sb) in zip(b.pop("mass"), s.pop("mass")):
         rel = max(rel, abs(br - sr) / abs(sr), abs(bb - sb) / abs(sb))
@@ -342,6 +409,8 @@ def serving_leg(mode: str, torch) -> dict:
             f"{n} requests, Poisson {rate:g}/s, bubble L in [32,192] or RTI LxLx4L L in [32,128] (log-uniform), "
             f"Q19/Q27 and FP32/FP16 by coin flip, steps U[500,5000] x {scale:g}",
             "batched": b, "sequential": s, "cases_per_s_ratio": b["cases_per_s"] / s["cases_per_s"],
+            "bound": bound, "bound_ratio": b["cases_per_s"] / bound["cases_per_s"],
+            "sequential_bound_ratio": s["cases_per_s"] / bound["cases_per_s"],
             "policy": "FIFO admission with backfill (all requests that fit are live)",
             "batched_sjf": {k: bs[k] for k in ("cases_per_s", "p50_s", "p99_s", "mlups", "makespan_s")},
             "batched_sjf_policy": "shortest job first with aging, live set capped at 4 waves of tiles",
@@ -390,6 +459,7 @@ def main() -> None:
     ap.add_argument("--q", type=int, default=27, choices=[27, 19], help="lattice of the jet (profiling the D3Q19 step)")
     ap.add_argument("--serving", default="sample", choices=["off", "sample", "full"])
     ap.add_argument("--no-configs", action="store_true", help="skip the bubble / RTI / D3Q19 lines")
+    ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's CUDA kernel")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -440,9 +510,11 @@ def main() -> None:
     e2e = time_e2e(p, args.e2e_steps, torch) if rank == 0 and args.e2e_steps > 0 else None
     serving = serving_leg(args.serving, torch) if rank == 0 and args.serving != "off" else None
     configs = configs_leg(torch) if rank == 0 and not args.no_configs else None
-    cpu = None
+    cpu = cpu64 = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_leg(args.cpu_budget, os.cpu_count() or 1)
+        cpu64 = cpu_leg(args.cpu_budget, os.cpu_count() or 1, real_bytes=8)
+    ref_cuda = reference_cuda_leg(args.steps, args.warmup, torch) if rank == 0 and not args.no_ref_cuda else None
 
     if rank == 0:
         out = {
@@ -452,7 +524,10 @@ def main() -> None:
             "data": "synthetic (analytic jet initial condition, seeded inlet noise)",
             "config": {"workload": (WORKLOAD if args.nz == 1024 else WORKLOAD.replace("x1024", f"x{args.nz}")).replace("D3Q27", f"D3Q{args.q}"), "lattice": [p.nx, p.ny, p.nz], "fluid_nodes": nodes,
                        "precision": "fp32 moments", "l2": "state 2x2.95 GB > 129 MB L2, no flush needed",
-                       "parallelism": "replicas" if world > 1 else "single GPU", "zchunk": os.environ.get("MBCG_ZCHUNK", "auto")},
+                       "parallelism": "replicas" if world > 1 else "single GPU", "zchunk": os.environ.get("MBCG_ZCHUNK", "auto"),
+                       "reference_arm_sample": "bench.py --impl reference times the reference arithmetic (FP32 "
+                                               "oracle) on the host cores over a 256x256x32-fluid-node z-slab of this "
+                                               "jet per step: the same per-node work, a 32-plane sample of the lattice"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_node": BYTES_PER_NODE[mbcg.FP32]},
@@ -461,6 +536,9 @@ def main() -> None:
             "configs": configs,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "cpu_baseline_fp64": cpu64,
+            "reference_cuda": ref_cuda,
+            "vs_reference_cuda": (mlups / world / ref_cuda["value"]) if ref_cuda and "value" in ref_cuda else None,
             "gpu_launches": args.steps * launches,
             "clocks": clk.summary(),
             "checks": {"mass_r": diag["mass_r"], "mass_b": diag["mass_b"], "nonfinite": diag["nonfinite"],

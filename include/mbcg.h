@@ -101,7 +101,11 @@ typedef struct mbcg_params {
                                still subtracts A|F|B_i/2, which does not sum to zero
                                (forces.cuh:80-83, collisionOperators.cuh:16-25); 1: Omega2 is
                                zero there, so colour masses are conserved exactly          */
-    int32_t reserved1;
+    int32_t wait_test_cycles; /* testing only, 0 in normal use.  > 0: the first plane wait of
+                               every step tile waits on a barrier that nothing completes, giving
+                               up after this many SM clock cycles, so the bounded-wait path runs:
+                               the tile drains its in-flight copies and exits, and mbcg_status
+                               reports 1 (the step's results are then incomplete)            */
     /* FP16/BF16 storage scales */
     double rho_scale;       /* (rho - rho_nominal) / rho_scale is stored; default 0.01     */
     double u_ref;           /* u / u_ref is stored; default 0.05                           */
@@ -185,7 +189,11 @@ int mbcg_run_host(mbcg_case *c, int32_t count, const float *const *in, float *co
 /* FP64 on-GPU conservation and Laplace-pressure diagnostics of state A (synchronous). */
 int mbcg_diagnostics(mbcg_case *c, mbcg_diag *out, mbcg_stream_t s);
 
-/* Reads and clears the device status word (non-zero = a bounded wait gave up). */
+/* Reads and clears the device status word.  0: every bounded device wait completed.  Bit 0
+ * (1): a wait for a staged plane gave up; the tile drained its in-flight copies and exited, so
+ * the step's results are incomplete but the context is usable.  Bit 1 (2): that drain gave up
+ * too, so copies may still have been writing into shared memory when the block exited: treat
+ * the context as poisoned (stop launching on it and report the error; do not re-run the step). */
 int mbcg_status(mbcg_case *c, int32_t *status);
 
 /* The parameters the case was created with. */
@@ -287,9 +295,10 @@ int mbcg_init_moments(const mbcg_params *p, const mbcg_moments *a, mbcg_stream_t
  * synchronise the device or fail under memory pressure), or code holding only MomentsDevice-style
  * arrays and no case handle.  The partial sums live in one fixed array compiled into the library
  * (about 385 KB, held on every GPU that loads it until the process exits); lattices above
- * 134,217,728 fluid nodes are rejected with MBCG_E_UNSUPPORTED.  The first call on each device
- * looks up that array's device address (with the device current), so make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race, so serialise them
+ * 134,217,728 fluid nodes are rejected with MBCG_E_UNSUPPORTED.  Every call looks up that
+ * array's device address with the calling thread's device current (so a device reset does not
+ * leave a stale address); the first call on a device also loads the library's device code
+ * there, so make it before any stream capture.  All calls share the array: calls that overlap on the GPU race, so serialise them
  * (same stream, or synchronise between them).  Synchronous: returns once *out is filled. */
 int mbcg_diagnostics_static(const mbcg_params *p, const mbcg_moments *a, mbcg_diag *out, mbcg_stream_t s);
 

@@ -90,6 +90,7 @@ void fill_physics(const mbcg_params& p, StepParams& P) {
     P.tau_b = p.tau_b > 0.0 ? static_cast<float>(p.tau_b) : taub;
     P.beta = static_cast<float>(p.beta);
     P.omega2_conservative = p.omega2_conservative != 0;
+    P.wait_test_cycles = p.wait_test_cycles > 0 ? p.wait_test_cycles : 0;
     P.ratio = p.rho_r0 != p.rho_b0;
     const double rmin = std::min(p.rho_r0, p.rho_b0);
     P.kappa_r = static_cast<float>(rmin / p.rho_r0 - 1.0);

@@ -169,6 +169,8 @@ struct StepParams {
     int ghost_images;   // the ghost frame of periodic x / y axes holds the periodic images of
                         // the opposite fluid layer (read by the step, written through on store)
     int* status;        // device status word (bounded-wait failures); may be null
+    int wait_test_cycles; // testing only: > 0 makes the first plane wait of a tile wait on a
+                          // barrier nothing completes, with this limit (exercises the bail path)
     const void* a[NF];  // current state
     void* b[NF];        // next state
 };

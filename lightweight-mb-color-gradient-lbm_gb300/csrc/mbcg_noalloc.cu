@@ -11,7 +11,6 @@
 
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "mbcg_internal.h"
@@ -26,32 +25,22 @@ constexpr int kMaxParts = 4096;
 constexpr long long kNodesPerBlock = 256LL * 128LL; // 256 threads, 128 fluid nodes each
 static __device__ __align__(256) double g_diag_scratch[(kMaxParts + 1) * kDiagSlots];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_scratch_addr[kMaxDevices] = {};
-
 int fail(int code, const std::string& msg) {
     set_last_error(msg); // reported by mbcg_last_error()
     return code;
 }
 
 // Device address of the scratch array on the current device.  The host-side symbol is only a
-// stand-in; the address must be queried per device with that device current.
+// stand-in; the address is looked up on every call, with the calling thread's device current,
+// so it stays valid after a cudaDeviceReset reloads the module at another address (the lookup
+// allocates nothing).
 int scratch_on_current_device(double** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(MBCG_E_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(MBCG_E_UNSUPPORTED, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_diag_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(MBCG_E_CUDA, std::string("cudaGetSymbolAddress of the diagnostics scratch: ") +
-                                         cudaGetErrorString(e));
-        g_scratch_addr[dev] = static_cast<double*>(p);
-    }
-    *out = g_scratch_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_diag_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(MBCG_E_CUDA, std::string("cudaGetSymbolAddress of the diagnostics scratch: ") +
+                                     cudaGetErrorString(e));
+    *out = static_cast<double*>(p);
     return MBCG_OK;
 }
 
@@ -63,6 +52,9 @@ extern "C" {
 // allocation; see include/mbcg.h for the contract.
 int mbcg_diagnostics_static(const mbcg_params* p, const mbcg_moments* a, mbcg_diag* out, mbcg_stream_t s) {
     if (!p || !a || !out) return fail(MBCG_E_INVALID, "null argument");
+    // precision tag, densities and sizes as every other entry point checks them (an unknown
+    // precision would otherwise read the fields with the wrong element size)
+    if (int rc = validate_params(p)) return rc;
     if (a->precision != p->precision) return fail(MBCG_E_INVALID, "moments precision differs from params");
     if (a->pitch < p->nx || p->nx < 3 || p->ny < 3 || p->nz < 3)
         return fail(MBCG_E_INVALID, "bad lattice size or pitch");

@@ -415,11 +415,12 @@ __device__ __forceinline__ unsigned char* aligned_smem_base() {
     return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
 }
 
-// Initialise the stage mbarriers (one elected thread) before the first tile of a CTA.
+// Initialise the stage mbarriers (one elected thread) before the first tile of a CTA.  One more
+// barrier after them is never arrived at: the bounded-wait test hook waits on it.
 __device__ __forceinline__ void init_stage_barriers(unsigned char* smem) {
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-        for (int s = 0; s < kNSTAGE; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s <= kNSTAGE; ++s) mbar_init(&bars[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -576,15 +577,18 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             return true;
         }
     };
-    // on a failed wait: flag it, drain the copies still in flight (bounded) and leave
+    // On a failed wait: drain the copies still in flight (bounded) and leave.  Status bit 0: a
+    // wait gave up; bit 1: the drain gave up too, so copies may still land in this block's
+    // shared memory after it exits (the host must treat the context as poisoned).
     auto bail = [&](int k_issued) {
-        if (tid == 0 && P.status) atomicOr(P.status, 1);
+        bool drained = true;
         if constexpr (kTMA) {
             for (int k = k_waited + 1; k <= k_issued; ++k) {
                 const int sl = (k - kfirst) % kNSTAGE;
-                mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit / 4);
+                drained = mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit / 4) && drained;
             }
         }
+        if (tid == 0 && P.status) atomicOr(P.status, drained ? 1 : 3);
     };
 
     // ---- psi ring: psi = (rhor - rhob)/rho (mathUtilities.cuh:12-19) of plane k over
@@ -639,6 +643,17 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     int k_issued = kfirst + kNSTAGE - 1;
     for (int k = kfirst; k <= k_issued; ++k) issue(k, k - kfirst);
     if constexpr (!kTMA) __syncthreads();
+    if constexpr (kTMA) {
+        if (P.wait_test_cycles > 0) {
+            // testing only: wait on the barrier nothing completes, so the wait runs out and the
+            // tile takes the bail path below with all its planes in flight
+            const bool ok = mbar_wait_bounded(&bars[kNSTAGE], 0u, P.wait_test_cycles);
+            if (__syncthreads_or(!ok)) {
+                bail(k_issued);
+                return false;
+            }
+        }
+    }
     {
         const bool ok = wait_slot(kfirst, 0) && wait_slot(kfirst + 1, 1);
         if (__syncthreads_or(!ok)) {

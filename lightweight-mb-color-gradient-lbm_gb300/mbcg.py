@@ -62,7 +62,7 @@ class Params(ctypes.Structure):
         ("rti_phase_above", ctypes.c_double),
         ("rti_mode", ctypes.c_int32 * 2),
         ("omega2_conservative", ctypes.c_int32),
-        ("reserved1", ctypes.c_int32),
+        ("wait_test_cycles", ctypes.c_int32),
         ("rho_scale", ctypes.c_double),
         ("u_ref", ctypes.c_double),
         ("pi_scale", ctypes.c_double),

@@ -23,7 +23,8 @@ import mbcg  # noqa: E402
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_SO = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 REF_DIR = os.path.join(ORACLE_DIR, "_ref")
-REF_ROOT = os.environ.get("MBCG_REF_ROOT", "/root/reference")
+# the reference checkout: MBCG_REF_ROOT, else a "reference" folder beside this repository
+REF_ROOT = os.environ.get("MBCG_REF_ROOT", os.path.join(os.path.dirname(ROOT), "reference"))
 
 _VP = ctypes.c_void_p
 _oracle = None

@@ -1,0 +1,92 @@
+"""Parity at the configurations' own sizes and horizons, against the FP64 oracle.
+
+The bubble and Rayleigh-Taylor configurations use model extensions the reference cannot express
+(fully periodic box and tanh bubble; walls, gravity and a density ratio), so their check is the
+FP64 oracle, itself pinned bit for bit to the reference's arithmetic on the golden fixtures.
+Gate (relative L2 per colour density, velocity field and stress field): 1e-5, or 3x the
+distance of the reference's FP32 arithmetic (the FP32 oracle) from the FP64 oracle where that
+is larger.
+
+* config 1, Rayleigh-Taylor 128 x 128 x 512 D3Q27 (walls at z = 0 and 511, density ratio 3,
+  gravity 1e-5, tau 0.55, sigma 5e-4): step 100 at full size; steps 5000 (and, with MBCG_LONG=1,
+  20000) on a 32 x 32 x 128 box with the same physics (the host oracle cannot run the full box
+  that long inside a test);
+* config 0, static bubble 64^3 D3Q19 (R 16, tanh width 3, tau 0.8, sigma 0.01, beta 0.7): the
+  moment fields, the Laplace pressure jump (within 1 % of the oracle's) and the phase masses at
+  step 2000.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import mbcg
+import oracle_lib as ol
+from gpu_util import assert_fp32_parity, gpu_run, written_nodes
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_pair(p, nsteps):
+    a = ol.oracle_init(p, np.float64)
+    o64 = ol.oracle_run(p, a.copy(), nsteps)
+    o32 = ol.oracle_run(p, a.astype(np.float32), nsteps)
+    return a, o64, o32
+
+
+def test_config1_rti_128x128x512_step100():
+    p = mbcg.rti_params(128, q=27)
+    assert (p.nx, p.ny, p.nz) == (130, 130, 512)
+    a, o64, o32 = _oracle_pair(p, 100)
+    got = gpu_run(p, a, 100)
+    eg, er = assert_fp32_parity(got, o64, o32, written_nodes(p), what="rti 128x128x512 step 100")
+    print(f"\nrti 128x128x512 step 100: gpu vs fp64 {eg}, fp32 oracle vs fp64 {er}")
+
+
+RTI_LONG = [5000] + ([20000] if os.environ.get("MBCG_LONG") else [])
+
+
+@pytest.mark.parametrize("nsteps", RTI_LONG)
+def test_config1_rti_physics_long_horizon(nsteps):
+    """The Rayleigh-Taylor physics on a 32 x 32 x 128 box; the instability amplifies round-off
+    (growth rate sqrt(A g k) ~ 1e-3 per step here), so the gate scales with the FP32 oracle's own
+    distance from the FP64 oracle."""
+    p = mbcg.rti_params(32, q=27)
+    a, o64, o32 = _oracle_pair(p, nsteps)
+    got = gpu_run(p, a, nsteps)
+    eg, er = assert_fp32_parity(got, o64, o32, written_nodes(p), what=f"rti 32x32x128 step {nsteps}")
+    print(f"\nrti 32x32x128 step {nsteps}: gpu vs fp64 {eg}, fp32 oracle vs fp64 {er}")
+
+
+def _laplace_dp(state, p):
+    f = state[:, 1:-1, 1:-1, 1:-1]
+    z, y, x = np.meshgrid(*[np.arange(1, n - 1) for n in (p.nz, p.ny, p.nx)], indexing="ij")
+    r2 = (x - p.bubble_center[0]) ** 2 + (y - p.bubble_center[1]) ** 2 + (z - p.bubble_center[2]) ** 2
+    pr = (f[0].astype(np.float64) + f[1]) / 3.0
+    rin, rout = 0.5 * p.bubble_radius, p.bubble_radius + 2 * p.bubble_width + 4
+    return pr[r2 <= rin ** 2].mean() - pr[r2 >= rout ** 2].mean()
+
+
+def test_config0_bubble_64_step2000():
+    p = mbcg.bubble_params(64, q=19)
+    a, o64, o32 = _oracle_pair(p, 2000)
+    with mbcg.Case(p) as c:
+        c.copy_in(a.astype(np.float32))
+        d0 = c.diagnostics()
+        c.step(2000)
+        got = c.copy_out()
+        d = c.diagnostics()
+        assert c.status() == 0
+    eg, er = assert_fp32_parity(got, o64, o32, written_nodes(p), what="bubble 64^3 step 2000")
+    dp_ref = _laplace_dp(o64, p)
+    assert dp_ref > 0
+    assert abs(d["dp"] - dp_ref) <= 0.01 * abs(dp_ref), (d["dp"], dp_ref)
+    # phase masses: the same change as the FP64 oracle's (the reference's Omega2 does not conserve
+    # colour mass below |F| = 1e-4), within 1 % of the oracle's change or 1e-6 of the mass
+    f0, f1 = a[:, 1:-1, 1:-1, 1:-1], o64[:, 1:-1, 1:-1, 1:-1]
+    for k, fi in (("mass_r", 0), ("mass_b", 1)):
+        m0 = f0[fi].sum()
+        ref_change = f1[fi].sum() - m0
+        gpu_change = d[k] - d0[k]
+        assert abs(gpu_change - ref_change) <= max(0.01 * abs(ref_change), 1e-6 * m0), (k, gpu_change, ref_change)
+    print(f"\nbubble 64^3 step 2000: gpu vs fp64 {eg}, fp32 oracle vs fp64 {er}; dp {d['dp']:.5e} vs {dp_ref:.5e}")

@@ -1,0 +1,58 @@
+"""Failure reporting of the fused step, made without faulting the GPU.
+
+* Bounded waits: every wait of the step for a staged plane gives up after a cycle limit and the
+  tile drains its in-flight copies before it exits.  The parameter field wait_test_cycles makes
+  the first wait of every tile wait on a barrier that nothing completes, with a short limit, so
+  that the wait runs out: the call returns, mbcg_status reports bit 0 (not bit 1: the drain
+  completed) and the context stays usable for the next case.
+* Non-finite states: a state seeded on the host with one node of zero density and one node
+  with a NaN velocity is counted by the diagnostics (2 nodes), and one step carries the NaN into
+  every destination of that node's populations (IEEE arithmetic: nothing in the step addresses
+  memory by a field value, so a bad value spreads but never faults).
+"""
+import numpy as np
+import pytest
+
+import mbcg
+import oracle_lib as ol
+from gpu_util import assert_fp32_parity, written_nodes
+
+pytestmark = pytest.mark.gpu
+
+
+def test_bounded_wait_runs_out_and_reports():
+    p = mbcg.reference_jet_params(34, 26, 22, q=27, tau=0.8, sigma=0.05, beta=0.7, radius=4.0)
+    p.wait_test_cycles = 200000  # about 0.1 ms of SM clock per tile
+    with mbcg.Case(p) as c:
+        c.init()
+        c.step(1)
+        assert c.status() == 1  # a wait gave up and the drain of in-flight copies completed
+        assert c.status() == 0  # mbcg_status clears the word
+    # the context is usable: the same case without the hook meets the parity gate
+    p.wait_test_cycles = 0
+    a0 = ol.oracle_init(p, np.float64)
+    ref64 = ol.oracle_run(p, a0.copy(), 5)
+    ref32 = ol.oracle_run(p, a0.astype(np.float32), 5)
+    with mbcg.Case(p) as c:
+        c.copy_in(a0.astype(np.float32))
+        c.step(5)
+        got = c.copy_out()
+        assert c.status() == 0
+    assert_fp32_parity(got, ref64, ref32, written_nodes(p), what="after a bounded-wait failure")
+
+
+@pytest.mark.parametrize("precision", [mbcg.FP32, mbcg.FP16])
+def test_bad_nodes_are_reported(precision):
+    p = mbcg.bubble_params(16, q=19, radius=4.0, precision=precision)
+    a = ol.oracle_init(p, np.float64).astype(np.float32)
+    a[0, 8, 7, 9] = 0.0     # rhor and rhob of one node: zero density
+    a[1, 8, 7, 9] = 0.0
+    a[2, 4, 11, 5] = np.nan  # ux of another node
+    with mbcg.Case(p) as c:
+        c.copy_in(a)
+        d0 = c.diagnostics()
+        c.step(1)
+        d1 = c.diagnostics()
+        assert c.status() == 0  # no wait gave up: bad data is not a stall
+    assert d0["nonfinite"] == 2, d0
+    assert d1["nonfinite"] >= 19, d1  # the NaN node's 19 destinations (itself included)

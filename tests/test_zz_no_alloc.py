@@ -33,7 +33,7 @@ def _close(a, b):
     assert a["nonfinite"] == b["nonfinite"] and a["nodes"] == b["nodes"]
 
 
-@pytest.mark.parametrize("precision", [mbcg.FP32, mbcg.FP16])
+@pytest.mark.parametrize("precision", [mbcg.FP32, mbcg.FP16, mbcg.BF16])
 def test_static_diagnostics_match_case_diagnostics(precision):
     lib = mbcg.Library.get()
     p = mbcg.bubble_params(40, q=27, radius=10.0, precision=precision)
