@@ -81,12 +81,18 @@ def test_config0_bubble_64_step2000():
     dp_ref = _laplace_dp(o64, p)
     assert dp_ref > 0
     assert abs(d["dp"] - dp_ref) <= 0.01 * abs(dp_ref), (d["dp"], dp_ref)
-    # phase masses: the same change as the FP64 oracle's (the reference's Omega2 does not conserve
-    # colour mass below |F| = 1e-4), within 1 % of the oracle's change or 1e-6 of the mass
-    f0, f1 = a[:, 1:-1, 1:-1, 1:-1], o64[:, 1:-1, 1:-1, 1:-1]
+    # phase masses: the same change as the FP64 oracle's.  The reference's Omega2 does not conserve
+    # colour mass below |F| = 1e-4 (the far field, where F is a difference of nearly equal psi
+    # values and FP32 round-off decides which nodes fall below the cut-off), so the gate is 1 % of
+    # the oracle's change or 3x the change of the reference's own FP32 arithmetic, whichever is larger
+    f0, f1, f32 = a[:, 1:-1, 1:-1, 1:-1], o64[:, 1:-1, 1:-1, 1:-1], o32[:, 1:-1, 1:-1, 1:-1]
     for k, fi in (("mass_r", 0), ("mass_b", 1)):
         m0 = f0[fi].sum()
         ref_change = f1[fi].sum() - m0
+        ref32_change = f32[fi].sum(dtype=np.float64) - m0
         gpu_change = d[k] - d0[k]
-        assert abs(gpu_change - ref_change) <= max(0.01 * abs(ref_change), 1e-6 * m0), (k, gpu_change, ref_change)
+        tol = max(0.01 * abs(ref_change), 3.0 * abs(ref32_change - ref_change))
+        print(f"\n{k} change over 2000 steps: gpu {gpu_change:.5e}, fp64 oracle {ref_change:.5e}, "
+              f"fp32 oracle {ref32_change:.5e}")
+        assert abs(gpu_change - ref_change) <= tol, (k, gpu_change, ref_change, ref32_change)
     print(f"\nbubble 64^3 step 2000: gpu vs fp64 {eg}, fp32 oracle vs fp64 {er}; dp {d['dp']:.5e} vs {dp_ref:.5e}")

@@ -5,7 +5,8 @@
   the first wait of every tile wait on a barrier that nothing completes, with a short limit, so
   that the wait runs out: the call returns, mbcg_status reports bit 0 (not bit 1: the drain
   completed) and the context stays usable for the next case.
-* Non-finite states: a state seeded on the host with one node of zero density and one node
+* Non-finite states: a state seeded on the host with one node of zero (FP32) or negative (16-bit
+  forms) density and one node
   with a NaN velocity is counted by the diagnostics (2 nodes), and one step carries the NaN into
   every destination of that node's populations (IEEE arithmetic: nothing in the step addresses
   memory by a field value, so a bad value spreads but never faults).
@@ -45,8 +46,12 @@ def test_bounded_wait_runs_out_and_reports():
 def test_bad_nodes_are_reported(precision):
     p = mbcg.bubble_params(16, q=19, radius=4.0, precision=precision)
     a = ol.oracle_init(p, np.float64).astype(np.float32)
-    a[0, 8, 7, 9] = 0.0     # rhor and rhob of one node: zero density
-    a[1, 8, 7, 9] = 0.0
+    # one node with a non-physical density: zero in FP32; in the 16-bit forms the stored slot is the
+    # scaled deviation from the nominal density, which decodes a zero density to ~1e-8 > 0, so a
+    # negative density stands in for it there
+    bad_rho = 0.0 if precision == mbcg.FP32 else -0.25
+    a[0, 8, 7, 9] = bad_rho  # rhor and rhob
+    a[1, 8, 7, 9] = bad_rho
     a[2, 4, 11, 5] = np.nan  # ux of another node
     with mbcg.Case(p) as c:
         c.copy_in(a)

@@ -139,34 +139,44 @@ def test_reference_cuda_jet_physics_reduced(jet_physics_gate):
     assert_within(e_pair, gate, "jet physics 64x128x64: library vs reference CUDA")
 
 
-def test_reference_cuda_jet_256x1024x256_100_steps(jet_physics_gate):
-    """The full jet lattice (258 x 1026 x 258), 100 steps, every group against the reference's
-    CUDA build, with the gate of the same physics on the reduced box (the FP64 oracle does not
-    fit a test at this size)."""
+def test_reference_cuda_jet_256x1024x256_100_steps():
+    """The full jet lattice (258 x 1026 x 258, jet along y), 100 steps, every group, against the
+    reference's CUDA build and the FP64 oracle.  Disturbances travel at most one node per step
+    from the inlet (the ambient rest state is a fixed point, bit for bit), so after 100 steps the
+    lattice beyond row 101 is still the initial state, and the FP64 oracle on a lattice cut at
+    row 113 (258 x 114 x 258, its outlet still at rest at step 100) gives the FP64 result of the
+    full lattice on rows 0..104, where the comparison with the oracle is made."""
     import torch
-    gate, _, _ = jet_physics_gate
     p = mbcg.reference_jet_params(258, 1026, 258, **JET_PHYS)
+    pc = mbcg.reference_jet_params(258, 114, 258, **JET_PHYS)
     k = RefKernels(_cubin("jet256"), (p.nx, p.ny, p.nz))
-    idx = written_nodes(p)
     with mbcg.Case(p) as c:
         c.init()
         init = c.copy_out()
         a, b = k.state(init), k.state(init)
-        del init
         for _ in range(100):
             k.step(a, b)
             a, b = b, a
         c.step(100)
         ours = c.copy_out()
         assert c.status() == 0
-    sl = idx[1:]
-    ref_t = [t.view(p.nz, p.ny, p.nx)[sl] for t in a]
-    ours_t = [torch.from_numpy(np.ascontiguousarray(ours[f][sl])).cuda() for f in range(11)]
-    del ours
-    e = _torch_group_errors(ours_t, ref_t)
-    print(f"\njet 256x1024x256, 100 steps: library vs reference CUDA {e}; gate {gate}")
-    assert e["rhor"] <= GATE and e["rhob"] <= GATE and e["u"] <= GATE, e
-    assert_within(e, gate, "jet 256x1024x256 step 100: library vs reference CUDA")
+    ref = k.host(a)
+    del a, b
+    torch.cuda.empty_cache()
+    # the cut lattice starts from the same state: the full lattice's first 114 rows (row 113, its
+    # outlet ghost, is ambient rest like every row beyond the inlet)
+    o64 = ol.oracle_run(pc, np.ascontiguousarray(init[:, :, :114, :]).astype(np.float64), 100)
+    idx = (slice(None), slice(1, -1), slice(0, 105), slice(1, -1))  # periodic x / z fluid nodes, rows 0..104
+    e_ref = group_errors(ref[idx], o64[idx])
+    gate = gates_from(e_ref)
+    e_ours = group_errors(ours[idx], o64[idx])
+    e_pair = group_errors(ours, ref, written_nodes(p))
+    moved = float(np.abs(ours[:, :, 110:-1, :] - init[:, :, 110:-1, :]).max())
+    print(f"\njet 256x1024x256 step 100: reference CUDA vs FP64 {e_ref}\n  library vs FP64 {e_ours}"
+          f"\n  library vs reference CUDA (whole lattice) {e_pair}\n  largest change beyond row 110: {moved:.3e}")
+    assert e_ours["rhor"] <= GATE and e_ours["rhob"] <= GATE, e_ours
+    assert_within(e_ours, gate, "jet 256x1024x256 step 100: library vs FP64 oracle")
+    assert_within(e_pair, gate, "jet 256x1024x256 step 100: library vs reference CUDA")
 
 
 REF_TIMING = {
