@@ -41,12 +41,12 @@ __global__ void __launch_bounds__(32 * W, 1)
         const long long step = cs.step0 + j + 1;
         bool ok = true;
         switch (C.kind) {
-        case BK_Q19_F32: ok = step_tile<19, float, W, true, F_ALL>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
-        case BK_Q19_F16: ok = step_tile<19, __half, W, true, F_ALL>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
-        case BK_Q19_BF16: ok = step_tile<19, __nv_bfloat16, W, true, F_ALL>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
-        case BK_Q27_F32: ok = step_tile<27, float, W, true, F_ALL>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
-        case BK_Q27_F16: ok = step_tile<27, __half, W, true, F_ALL>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
-        case BK_Q27_BF16: ok = step_tile<27, __nv_bfloat16, W, true, F_ALL>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
+        case BK_Q19_F32: ok = step_tile<19, float, W, true, F_ALL, false>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
+        case BK_Q19_F16: ok = step_tile<19, __half, W, true, F_ALL, false>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
+        case BK_Q19_BF16: ok = step_tile<19, __nv_bfloat16, W, true, F_ALL, false>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
+        case BK_Q27_F32: ok = step_tile<27, float, W, true, F_ALL, false>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
+        case BK_Q27_F16: ok = step_tile<27, __half, W, true, F_ALL, false>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
+        case BK_Q27_BF16: ok = step_tile<27, __nv_bfloat16, W, true, F_ALL, false>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
         case BK_Q19_F32_P: ok = step_tile<19, float, W, true, 0>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
         case BK_Q19_F16_P: ok = step_tile<19, __half, W, true, 0>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
         case BK_Q27_F32_P: ok = step_tile<27, float, W, true, 0>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;

@@ -430,7 +430,9 @@ __device__ __forceinline__ void init_stage_barriers(unsigned char* smem) {
 // is the index of the state being written (keys the inlet noise); `phase` carries the parity
 // of the stage mbarriers from one tile of a CTA to the next (0 before the first tile).
 // Returns false if a staged plane never arrived (the status word is set and the CTA must stop).
-template <int Q, typename S, int W, bool kTMA, int kFeat>
+// kLeanZ: compile the steady-state body for an inlet/outlet z axis (the batch kernel, whose
+// lattices never have one, leaves it out).
+template <int Q, typename S, int W, bool kTMA, int kFeat, bool kLeanZ = true>
 __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap* maps, int bx, int by, int bz,
                                           long long step, unsigned char* smem, uint32_t& phase) {
     using G = Geo<S, W>;
@@ -497,6 +499,13 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         if (e < G::psi_plane) {
             const int r = e / kPSX, c = e % kPSX;
             const int gx = xb - 1 + c, gy = yb - 1 + r;
+            if (gx < -1 || gx > nx || gy < -1 || gy > ny) {
+                // beyond the ghost frame and its one-node halo: read only by the colour gradient of
+                // sources outside the lattice, whose populations reach no destination of the tile,
+                // so any staged element serves (no global load)
+                psi_box[j] = 0;
+                continue;
+            }
             const int mx = psi_coord(P, 0, gx, nx), my = psi_coord(P, 1, gy, ny);
             const bool px = P.bc[0] == MBCG_BC_PERIODIC, py = P.bc[1] == MBCG_BC_PERIODIC;
             const int dx = (px && gx >= 0 && gx <= nx - 1) ? gx : mx;
@@ -677,7 +686,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     float4* xb_self = xbuf + w * 32 + lane; // (X0, XR, X1, X2) of one exported row
 
     int sl = 1; // slot of plane k (k starts at kfirst + 1)
-    for (int k = zd0 - 1; k <= zd1; ++k, sl = nxt(sl)) {
+    int k = zd0 - 1;
+    // One plane of the z-march with the feature set kFB: the tile's own, or, on the steady-state
+    // planes of an inlet/outlet z axis, the same set without the inlet/outlet parts.  Returns false
+    // after a bail.
+    auto plane = [&](auto featc) -> bool {
+        constexpr int kFB = decltype(featc)::value;
         const int sl_next = nxt(sl), sl_prev = prv(sl);
         // (1) psi of plane k+1; one barrier both publishes the ring and makes the bail decision
         // uniform (a plane that never arrived leaves garbage in the ring, which nobody reads)
@@ -690,7 +704,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             mz1 = psi_coord(P, 2, k + 1, nz);
             inbox1 = mz1 == zload(k + 1);
             mz2 = psi_coord(P, 2, k + 2, nz);
-            rz = axis_role<kFeat>(P, 2, k, nz);
+            rz = axis_role<kFB>(P, 2, k, nz);
         }
         {
             const bool ok = wait_slot(k + 1, sl_next);
@@ -712,7 +726,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         // Sources outside the lattice (lanes / rows past the last ghost layer) only ever stream
         // into nodes that are not destinations of this tile, so without walls every source is
         // processed branch-free; wall ghost layers hold data and must not emit.
-        const bool active = ((kFeat & F_WALL) == 0) || (role == R_FLUID || role == R_GHOST);
+        const bool active = ((kFB & F_WALL) == 0) || (role == R_FLUID || role == R_GHOST);
 
         unsigned char* st = stage_at(sl);
         Node<S> nd{};
@@ -724,7 +738,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
 #pragma unroll
             for (int f = 2; f < NF; ++f) v[f] = Codec<S>::to_f(m_box(st, f)[bM]);
             decode<S>(P, v, nd);
-            if constexpr ((kFeat & F_INOUT) != 0) {
+            if constexpr ((kFB & F_INOUT) != 0) {
                 if (role == R_GHOST) {
                     // the first fluid node behind the ghost: plane 1 or nz-2 (still staged: the
                     // slot of plane nz-2 is not refilled in the chunk that ends at nz-1), or the
@@ -761,15 +775,15 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             const float q0 = nd.rr * inv;
             const float q1 = fmaf(fmaf(-q0, rho, nd.rr), inv, q0);
             aR = nd.rb == 0.0f ? 1.0f : (nd.rr == 0.0f ? 0.0f : q1);
-            if (!(kFeat & F_INOUT) || role == R_FLUID) {
+            if (!(kFB & F_INOUT) || role == R_FLUID) {
                 iface = (4.0f * nd.rr * nd.rb * inv * inv) > 1.0e-4f; // lbm.cuh:181,187
                 // zero-filled staging outside the lattice decodes to a mixed node in the 16-bit
                 // forms; keep those (never written) sources off the interface path
                 if constexpr (sizeof(S) != 4) iface = iface && in_xy;
-                build_coef<kFeat>(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, nd.ux, nd.uy, nd.uz, nd.pxx, nd.pxy,
+                build_coef<kFB>(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, nd.ux, nd.uy, nd.uz, nd.pxx, nd.pxy,
                                   nd.pyy, nd.pyz, nd.pzz, nd.pxz);
             } else {
-                build_coef<kFeat>(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, fn.ux, fn.uy, fn.uz, fn.pxx, fn.pxy,
+                build_coef<kFB>(P, cf, rho, nd.rr, nd.rb, nd.ux, nd.uy, nd.uz, fn.ux, fn.uy, fn.uz, fn.pxx, fn.pxy,
                                   fn.pyy, fn.pyz, fn.pzz, fn.pxz);
             }
         }
@@ -803,7 +817,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             const float absF = sqrtf(Fx * Fx + Fy * Fy + Fz * Fz);
             // Omega2 (collisionOperators.cuh:16-25) folded into the coefficients
             float Aeff = P.A; // A_calculation (forces.cuh:114-117) at the node's relaxation time
-            if constexpr ((kFeat & F_FORCE) != 0)
+            if constexpr ((kFB & F_FORCE) != 0)
                 if (P.tau_var) Aeff = P.s4 / tau_eff_of(P, nd.rr, nd.rb);
             float hA = (P.omega2_conservative && !(absF > 1.0e-4f)) ? 0.0f : 0.5f * Aeff * absF;
             if (absF > 1.0e-4f) {
@@ -821,7 +835,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 // recolouring (collisionOperators.cuh:60-80): beta rr rb / (rho^2 |F|) * feq0, where
                 // the rest equilibrium of moving directions is w rho (w (rho + K) with a density ratio)
                 const float rho = nd.rr + nd.rb;
-                const float feq0 = ((kFeat & F_FORCE) && P.ratio) ? rho + nd.rr * P.kappa_r + nd.rb * P.kappa_b : rho;
+                const float feq0 = ((kFB & F_FORCE) && P.ratio) ? rho + nd.rr * P.kappa_r + nd.rb * P.kappa_b : rho;
                 const float irho = fast_rcp(rho);
                 dcoef = P.beta * (nd.rr * nd.rb) * irho * irho * ia_ * feq0;
             }
@@ -864,8 +878,8 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         const bool wx0 = P.bc[0] == MBCG_BC_WALL && xs == 1, wx1 = P.bc[0] == MBCG_BC_WALL && xs == nx - 2;
         const bool wy0 = P.bc[1] == MBCG_BC_WALL && ys == 1, wy1 = P.bc[1] == MBCG_BC_WALL && ys == ny - 2;
         const bool wz0 = P.bc[2] == MBCG_BC_WALL && k == 1, wz1 = P.bc[2] == MBCG_BC_WALL && k == nz - 2;
-        const bool reflect = (kFeat & F_WALL) && role == R_FLUID && dest_thread && (wx0 | wx1 | wy0 | wy1 | wz0 | wz1);
-        const bool any_reflect = (kFeat & F_WALL) ? __any_sync(kFull, reflect) : false;
+        const bool reflect = (kFB & F_WALL) && role == R_FLUID && dest_thread && (wx0 | wx1 | wy0 | wy1 | wz0 | wz1);
+        const bool any_reflect = (kFB & F_WALL) ? __any_sync(kFull, reflect) : false;
 
         // ---- emit: populations of the rows this warp exports, x streaming, own-row moments,
         // y exchange.  Halo rows export one population row (cy = +1 for warp 0, -1 for warp W-1).
@@ -923,7 +937,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                     const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
                     return dks * fc;
                 };
-                if constexpr (ROWS == 7 && (kFeat & F_WALL) != 0) {
+                if constexpr (ROWS == 7 && (kFB & F_WALL) != 0) {
                     if (any_reflect && reflect) {
 #pragma unroll
                         for (int i = 0; i < 3; ++i)
@@ -1077,7 +1091,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             const float rb = rho - rr;
             const float inv = fast_rcp(rho);
             float Fbx = 0.0f, Fby = 0.0f, Fbz = 0.0f;
-            constexpr bool kF = (kFeat & F_FORCE) != 0;
+            constexpr bool kF = (kFB & F_FORCE) != 0;
             if (kF && P.forced) {
                 Fbx = rho * P.g[0];
                 Fby = rho * P.g[1];
@@ -1110,7 +1124,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             }
             finalize_store<S>(P, xs, ys, d, rr, rb, ux, uy, uz, pi, img_x, img_y, key_base);
 
-            if ((kFeat & F_INOUT) && (bc_xy || (bc_z && (d == 1 || d == nz - 2)))) {
+            if ((kFB & F_INOUT) && (bc_xy || (bc_z && (d == 1 || d == nz - 2)))) {
                 // inlet / outlet functors fused into the first and last fluid layer
                 const int pa = ia == 0 ? xs : (ia == 1 ? ys : d);
                 {
@@ -1182,7 +1196,28 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
         }
         accP = accC;
         accC = accN; // accN is assigned before it is added to again
+            return true;
+    };
+    auto run = [&](auto featc, int kend) -> bool {
+        for (; k <= kend; ++k, sl = nxt(sl))
+            if (!plane(featc)) return false;
+        return true;
+    };
+    if constexpr ((kFeat & F_INOUT) != 0 && kLeanZ) {
+        // With the inlet/outlet axis along z, planes 3 .. nz-5 need none of its parts: their sources
+        // (planes k .. k+3 staged) are fluid planes with identity mappings, and the destination plane
+        // k-1 is neither of the layers the inlet / outlet functors write.  Which body a plane runs
+        // depends on k only, so results do not depend on the z chunking.  (An x / y inlet-outlet
+        // axis keeps the full body everywhere: there the choice would depend on the tile shape.)
+        if (ia == 2) {
+            const int k0 = max(zd0 - 1, 3), k1 = min(zd1, nz - 5);
+            if (k1 >= k0) {
+                if (!run(std::integral_constant<int, kFeat>{}, k0 - 1)) return false;
+                if (!run(std::integral_constant<int, kFeat & ~F_INOUT>{}, k1)) return false;
+            }
+        }
     }
+    if (!run(std::integral_constant<int, kFeat>{}, zd1)) return false;
     // every load of this tile was waited for: carry the parities over to the next tile
     phase = par;
     return true;
