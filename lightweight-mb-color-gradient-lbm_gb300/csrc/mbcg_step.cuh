@@ -1203,17 +1203,15 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             if (!plane(featc)) return false;
         return true;
     };
-    if constexpr ((kFeat & F_INOUT) != 0 && kLeanZ) {
-        // With the inlet/outlet axis along z, planes 3 .. nz-5 need none of its parts: their sources
-        // (planes k .. k+3 staged) are fluid planes with identity mappings, and the destination plane
-        // k-1 is neither of the layers the inlet / outlet functors write.  Which body a plane runs
-        // depends on k only, so results do not depend on the z chunking.  (An x / y inlet-outlet
-        // axis keeps the full body everywhere: there the choice would depend on the tile shape.)
-        if (ia == 2) {
-            const int k0 = max(zd0 - 1, 3), k1 = min(zd1, nz - 5);
+    if constexpr ((kFeat & (F_INOUT | F_WALL)) != 0 && kLeanZ) {
+        // The inlet/outlet or wall axis along z: planes 3 (walls: 2) .. nz-5 need none of its parts
+        // (fluid sources with identity mappings, no wall-adjacent source, no functor store).
+        const bool zin = ia == 2, zwall = P.bc[2] == MBCG_BC_WALL;
+        if (zin || zwall) {
+            const int k0 = max(zd0 - 1, zin ? 3 : 2), k1 = min(zd1, nz - 5);
             if (k1 >= k0) {
                 if (!run(std::integral_constant<int, kFeat>{}, k0 - 1)) return false;
-                if (!run(std::integral_constant<int, kFeat & ~F_INOUT>{}, k1)) return false;
+                if (!run(std::integral_constant<int, kFeat & ~(F_INOUT | F_WALL)>{}, k1)) return false;
             }
         }
     }
