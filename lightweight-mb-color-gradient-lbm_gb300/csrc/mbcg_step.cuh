@@ -590,14 +590,14 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     // wait gave up; bit 1: the drain gave up too, so copies may still land in this block's
     // shared memory after it exits (the host must treat the context as poisoned).
     auto bail = [&](int k_issued) {
-        bool drained = true;
+        if (tid == 0 && P.status) atomicOr(P.status, 1);
         if constexpr (kTMA) {
             for (int k = k_waited + 1; k <= k_issued; ++k) {
                 const int sl = (k - kfirst) % kNSTAGE;
-                drained = mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit / 4) && drained;
+                if (!mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit / 4) && tid == 0 && P.status)
+                    atomicOr(P.status, 2);
             }
         }
-        if (tid == 0 && P.status) atomicOr(P.status, drained ? 1 : 3);
     };
 
     // ---- psi ring: psi = (rhor - rhob)/rho (mathUtilities.cuh:12-19) of plane k over
@@ -652,19 +652,22 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
     int k_issued = kfirst + kNSTAGE - 1;
     for (int k = kfirst; k <= k_issued; ++k) issue(k, k - kfirst);
     if constexpr (!kTMA) __syncthreads();
-    if constexpr (kTMA) {
-        if (P.wait_test_cycles > 0) {
-            // testing only: wait on the barrier nothing completes, so the wait runs out and the
-            // tile takes the bail path below with all its planes in flight
-            const bool ok = mbar_wait_bounded(&bars[kNSTAGE], 0u, P.wait_test_cycles);
-            if (__syncthreads_or(!ok)) {
-                bail(k_issued);
-                return false;
+    {
+        // The first wait.  Testing only (wait_test_cycles > 0): it waits on the barrier nothing
+        // completes, with that limit, so it runs out and the tile takes the bail path with all its
+        // planes in flight.  (Folded into the one wait: a second wait-and-bail path at the tile
+        // start cost the ten-body batch kernel ~20 %.)
+        bool ok = true;
+        if constexpr (kTMA) {
+            const bool test = P.wait_test_cycles > 0;
+            ok = mbar_wait_bounded(test ? &bars[kNSTAGE] : &bars[0], test ? 0u : (par & 1u),
+                                   test ? static_cast<long long>(P.wait_test_cycles) : kWaitLimit);
+            if (ok) {
+                par ^= 1u;
+                k_waited = kfirst;
             }
         }
-    }
-    {
-        const bool ok = wait_slot(kfirst, 0) && wait_slot(kfirst + 1, 1);
+        ok = ok && wait_slot(kfirst + 1, 1);
         if (__syncthreads_or(!ok)) {
             bail(k_issued);
             return false;
