@@ -69,6 +69,9 @@ def test_storage_form_error_vs_fp64(oracle_states, prec, tol100, tol1000):
     if prec == mbcg.FP16:
         for k in ("rhor", "rhob", "u"):
             assert e100[k] < FORM_TARGET and e1000[k] < FORM_TARGET, (k, e100, e1000)
+        if not (e100["Pi"] < FORM_TARGET and e1000["Pi"] < FORM_TARGET):
+            pytest.xfail(f"FP16 stress field {e100['Pi']:.1e} (100 steps) / {e1000['Pi']:.1e} (1000 steps) above "
+                         f"the 1e-3 target: the 16-bit velocity's rounding enters Pi through rho u u")
 
 
 def test_stochastic_rounding_is_reproducible():
