@@ -50,3 +50,20 @@ def test_native_line_reduced():
     assert {"sm_mhz", "sm_max_mhz", "reasons"} <= set(d["clocks"])
     assert d["checks"]["nonfinite"] == 0 and d["checks"]["status"] == 0
     assert "x64 " in d["config"]["workload"]
+
+
+def test_serving_bound_arithmetic():
+    """The cases/s ceiling of a request stream at the plain kernel's per-request times: the makespan
+    of the best preemptive one-at-a-time schedule with those release times."""
+    import bench
+    reqs = [{"t": 0.0}, {"t": 1.0}, {"t": 2.0}]
+    # work-bound: everything released early, 7 s of work
+    b = bench.serving_bound(reqs, [5.0, 1.0, 1.0])
+    assert abs(b["makespan_s"] - 7.0) < 1e-12 and abs(b["cases_per_s"] - 3 / 7.0) < 1e-12
+    # release-bound: the last request arrives late, after the rest is done
+    reqs2 = [{"t": 0.0}, {"t": 1.0}, {"t": 10.0}]
+    b2 = bench.serving_bound(reqs2, [1.0, 1.0, 0.5])
+    assert abs(b2["makespan_s"] - 10.5) < 1e-12
+    # order of the list does not matter (sorted by release time)
+    b3 = bench.serving_bound(list(reversed(reqs2)), [0.5, 1.0, 1.0])
+    assert abs(b3["makespan_s"] - 10.5) < 1e-12
