@@ -36,8 +36,8 @@ def test_bubble_mass_conservation_10k_steps():
 
     The blue (bulk) phase meets it.  The red (bubble) phase does not: its colour sums are O(1)
     numbers across the whole diffuse interface (the tanh profile keeps both colours present
-    within ~16 nodes of the bubble), and their FP32 rounding, frozen in the near-steady state,
-    drifts the red mass by ~7e-6.  The floor of FP32 storage itself, measured with FP64
+    within ~16 nodes of the bubble), and their FP32 arithmetic drifts the red mass by ~7e-6,
+    linearly from the first step (a bias: randomising the inputs by +-1 ulp barely changes it).  The floor of FP32 storage itself, measured with FP64
     arithmetic and the state rounded to FP32 after every step
     (tests/test_mass_floor.py, opt-in), is 6.9e-7 for red and 8.6e-8 for blue, so the gap is
     this kernel's FP32 arithmetic, not the storage.  The test asserts blue < 1e-6 and red < 1e-5
