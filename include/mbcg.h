@@ -189,11 +189,12 @@ int mbcg_run_host(mbcg_case *c, int32_t count, const float *const *in, float *co
 /* FP64 on-GPU conservation and Laplace-pressure diagnostics of state A (synchronous). */
 int mbcg_diagnostics(mbcg_case *c, mbcg_diag *out, mbcg_stream_t s);
 
-/* Reads and clears the device status word.  0: every bounded device wait completed.  Bit 0
- * (1): a wait for a staged plane gave up; the tile drained its in-flight copies and exited, so
- * the step's results are incomplete but the context is usable.  Bit 1 (2): that drain gave up
- * too, so copies may still have been writing into shared memory when the block exited: treat
- * the context as poisoned (stop launching on it and report the error; do not re-run the step). */
+/* Reads and clears the device status word.  0: every bounded device wait completed.  1: a wait
+ * for a staged plane gave up; the tile then drained its in-flight copies with a bounded wait and
+ * exited, so the step's results are incomplete.  Should that drain have given up as well, copies
+ * could still land in shared memory after the block exited, and the word cannot tell the two
+ * cases apart: treat any non-zero status as a poisoned context (stop launching on it, report the
+ * error, do not re-run the step). */
 int mbcg_status(mbcg_case *c, int32_t *status);
 
 /* The parameters the case was created with. */

@@ -586,16 +586,16 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             return true;
         }
     };
-    // On a failed wait: drain the copies still in flight (bounded) and leave.  Status bit 0: a
-    // wait gave up; bit 1: the drain gave up too, so copies may still land in this block's
-    // shared memory after it exits (the host must treat the context as poisoned).
+    // On a failed wait: flag it, drain the copies still in flight (bounded) and leave.  If the drain
+    // gives up too, copies may still land in this block's shared memory after it exits, which the
+    // status cannot tell apart (a flag for it cost the ten-body batch kernel 3-5 %): the host treats
+    // any non-zero status as a poisoned context.
     auto bail = [&](int k_issued) {
         if (tid == 0 && P.status) atomicOr(P.status, 1);
         if constexpr (kTMA) {
             for (int k = k_waited + 1; k <= k_issued; ++k) {
                 const int sl = (k - kfirst) % kNSTAGE;
-                if (!mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit / 4) && tid == 0 && P.status)
-                    atomicOr(P.status, 2);
+                mbar_wait_bounded(&bars[sl], (par >> sl) & 1u, kWaitLimit / 4);
             }
         }
     };

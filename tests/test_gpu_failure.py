@@ -3,8 +3,9 @@
 * Bounded waits: every wait of the step for a staged plane gives up after a cycle limit and the
   tile drains its in-flight copies before it exits.  The parameter field wait_test_cycles makes
   the first wait of every tile wait on a barrier that nothing completes, with a short limit, so
-  that the wait runs out: the call returns, mbcg_status reports bit 0 (not bit 1: the drain
-  completed) and the context stays usable for the next case.
+  that the wait runs out: the call returns and mbcg_status reports 1.  The real copies complete, so
+  the drain completes and the context stays usable for the next case (in general a non-zero
+  status marks the context as poisoned, because the drain is itself bounded).
 * Non-finite states: a state seeded on the host with one node of zero (FP32) or negative (16-bit
   forms) density and one node
   with a NaN velocity is counted by the diagnostics (2 nodes), and one step carries the NaN into
@@ -27,7 +28,7 @@ def test_bounded_wait_runs_out_and_reports():
     with mbcg.Case(p) as c:
         c.init()
         c.step(1)
-        assert c.status() == 1  # a wait gave up and the drain of in-flight copies completed
+        assert c.status() == 1  # a wait gave up (the tile drained its in-flight copies)
         assert c.status() == 0  # mbcg_status clears the word
     # the context is usable: the same case without the hook meets the parity gate
     p.wait_test_cycles = 0
