@@ -846,6 +846,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             omega2_rest = hA; // rest-population part, -hA (B0 - w0) = +2/3 hA, added below in exact units
         }
         const float rho_src = active ? nd.rr + nd.rb : 0.0f;
+        const float rr_src = active ? nd.rr : 0.0f;
         // colour fractions of the x neighbours (lane -1 and lane +1)
         float2 aRlr;
         aRlr.x = __shfl_up_sync(kFull, aR, 1);
@@ -911,22 +912,25 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
             }
             auto do_class = [&](auto czc, Acc& acc) {
                 constexpr int cz = decltype(czc)::value;
-                // populations of row j: rho + the small part (rho last, see above)
-                Tri g[3];
+                // populations of row j: rho + the small part (rho last, see above); sm keeps the
+                // small parts (value units, before the D3Q19 weight) for the red populations
+                Tri g[3], sm[3];
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     const int cy = j - 1;
-                    g[j].o = make_float2(0.0f, 0.0f);
-                    g[j].c = 0.0f;
+                    g[j].o = sm[j].o = make_float2(0.0f, 0.0f);
+                    g[j].c = sm[j].c = 0.0f;
                     if (!(ROWS & (1 << j))) continue;
                     Tri small = cz == 0 ? s0[j] : (cz > 0 ? e2[j] + s1[j] : e2[j] - s1[j]);
                     if (cy == 0 && cz == 0) small.c += rc0;
                     const int shc = cy * cy + cz * cz; // |c|^2 of the centre; the outer ones have shc + 1
                     if (Stencil<Q>::has(1, cy, cz)) {
+                        sm[j].o = small.o;
                         const float2 vv = __fadd2_rn(rho2, small.o);
                         g[j].o = (kSepW || shc != 0) ? vv : __fadd2_rn(vv, vv);
                     }
                     if (Stencil<Q>::has(0, cy, cz)) {
+                        sm[j].c = small.c;
                         const float vv = rho_src + small.c;
                         g[j].c = kSepW ? vv : (shc == 0 ? 12.0f * vv : (shc == 1 ? vv + vv : vv));
                     }
@@ -939,6 +943,25 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                     const float dks = sh == 1 ? dk1 : (sh == 2 ? dk2 : dk3);
                     const float fc = (cx ? cx * Fx : 0.0f) + (cy ? cy * Fy : 0.0f) + (cz ? cz * Fz : 0.0f);
                     return dks * fc;
+                };
+                // Red population of direction (cx, cy, cz) = (i - 1, j - 1, cz) of a source with
+                // density rho, red density rr, colour fraction aR = rr / rho, population
+                // g = W (rho + sm) and recolouring part Delta.  On interface warps it is formed
+                // as W (rr + aR sm) + Delta, which is aR g + Delta in exact arithmetic but sums
+                // to S rr over the source's directions whatever the rounding of aR (sm sums to
+                // zero): near rho = 1, rr / rho lies within an ulp of rr and rounds with the sign
+                // of rho - 1 (the Laplace pressure of a bubble), so aR g would move colour mass
+                // the same way every step (red drift 7e-6 instead of 3.5e-7 over 10^4 steps of
+                // the 64^3 D3Q19 bubble).  Elsewhere aR is within 2.5e-5 of 0 or 1 and the
+                // populations are aR g.
+                auto red_pop = [&](float rr_, float smv, float gv, float dl, int i, int j, bool withd) -> float {
+                    if (!withd) return aR * gv;
+                    const int cy = j - 1, shc = cy * cy + cz * cz + (i != 1 ? 1 : 0);
+                    const float b = fmaf(aR, smv, rr_);
+                    // D3Q19 weight of the population: 12 (rest), 2 (|c|^2 = 1), 1 (|c|^2 = 2)
+                    if (kSepW || shc == 2) return b + dl;
+                    if (shc == 1) return fmaf(2.0f, b, dl);
+                    return fmaf(12.0f, b, dl);
                 };
                 if constexpr (ROWS == 7 && (kFB & F_WALL) != 0) {
                     if (any_reflect && reflect) {
@@ -955,15 +978,16 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                                                                            (cz == 0 ? 4 : 1))
                                                       : 1.0f;
                                 const float gv = i == 0 ? g[j].o.x : (i == 2 ? g[j].o.y : g[j].c);
-                                const float rr_ = any_iface ? fmaf(aR, gv, delta(i, j)) : aR * gv;
+                                const float smv = i == 0 ? sm[j].o.x : (i == 2 ? sm[j].o.y : sm[j].c);
+                                const float rr_ = red_pop(rr_src, smv, gv, any_iface ? delta(i, j) : 0.0f, i, j, any_iface);
                                 add_pop(accC, f * gv, f * rr_, -cx, -cy, -cz);
                             }
                     }
                 }
                 // x streaming: destination x receives cx=+1 from lane-1 and cx=-1 from lane+1.
-                // Only g crosses lanes: the destination forms each red population aR g (+ Delta)
-                // itself from the source's colour fraction (shuffled once per plane), with the
-                // very operations the source would use, so the red sums are the same bits.
+                // The populations cross lanes; on interface warps the source forms its red
+                // populations (red_pop) and they cross too, elsewhere the destination forms them
+                // as aR g from the source's colour fraction (shuffled once per plane).
                 float X0[3], X1[3], X2[3], XR[3];
                 auto xstream = [&](auto ifc) {
                     constexpr bool kIf = decltype(ifc)::value;
@@ -972,7 +996,7 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                         const int cy = j - 1;
                         X0[j] = X1[j] = X2[j] = XR[j] = 0.0f;
                         if (!(ROWS & (1 << j))) continue;
-                        const float r1 = kIf ? fmaf(aR, g[j].c, delta(1, j)) : aR * g[j].c;
+                        const float r1 = red_pop(rr_src, sm[j].c, g[j].c, kIf ? delta(1, j) : 0.0f, 1, j, kIf);
                         if (Stencil<Q>::has(1, cy, cz)) {
                             float2 glr; // (from lane - 1, from lane + 1)
                             glr.x = __shfl_up_sync(kFull, g[j].o.y, 1);
@@ -982,10 +1006,13 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                             X1[j] = glr.x - glr.y;
                             float2 rlr;
                             if constexpr (kIf) {
-                                float2 qlr;
-                                qlr.x = __shfl_up_sync(kFull, delta(2, j), 1);
-                                qlr.y = __shfl_down_sync(kFull, delta(0, j), 1);
-                                rlr = __ffma2_rn(aRlr, glr, qlr);
+                                // red_pop of this lane's cx = -1 / +1 populations, paired
+                                const bool w2 = !kSepW && cy == 0 && cz == 0; // D3Q19 weight 2
+                                float2 ro = __ffma2_rn(pair(aR), sm[j].o, pair(rr_src));
+                                const float2 dl = make_float2(delta(0, j), delta(2, j));
+                                ro = w2 ? __ffma2_rn(pair(2.0f), ro, dl) : __fadd2_rn(ro, dl);
+                                rlr.x = __shfl_up_sync(kFull, ro.y, 1);
+                                rlr.y = __shfl_down_sync(kFull, ro.x, 1);
                             } else {
                                 rlr = __fmul2_rn(aRlr, glr);
                             }

@@ -1,6 +1,6 @@
 """The phase-mass floor of FP32 state storage on the 64^3 D3Q19 bubble (conservative Omega2),
 10^4 steps: the FP64 oracle's arithmetic with the state rounded to FP32 after every step.  This
-separates what FP32 storage costs from what FP32 arithmetic costs (the GPU's red-phase drift,
+separates what FP32 storage costs from what FP32 arithmetic costs (the GPU's phase drift,
 tests/test_gpu_diagnostics.py).  Measured on 6 host threads (about 27 min): red +6.9e-7,
 blue +8.6e-8.  Opt-in: MBCG_LONG=1.
 """
