@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(32 * W, 1)
         case BK_Q27_F16_P: ok = step_tile<27, __half, W, true, 0>(sP, maps, bt.bx, bt.by, bt.bz, step, smem, phase); break;
         default: ok = false; break;
         }
-        if (!ok) return; // step_tile has set the lattice's status word (bit 0, or bits 0-1)
+        if (!ok) return; // step_tile has set the lattice's status word
     }
 }
 
