@@ -947,12 +947,12 @@ __device__ __forceinline__ bool step_tile(const StepParams& P, const CUtensorMap
                 // Red population of direction (cx, cy, cz) = (i - 1, j - 1, cz) of a source with
                 // density rho, red density rr, colour fraction aR = rr / rho, population
                 // g = W (rho + sm) and recolouring part Delta.  On interface warps it is formed
-                // as W (rr + aR sm) + Delta, which is aR g + Delta in exact arithmetic but sums
-                // to S rr over the source's directions whatever the rounding of aR (sm sums to
-                // zero): near rho = 1, rr / rho lies within an ulp of rr and rounds with the sign
-                // of rho - 1 (the Laplace pressure of a bubble), so aR g would move colour mass
-                // the same way every step (red drift 7e-6 instead of 3.5e-7 over 10^4 steps of
-                // the 64^3 D3Q19 bubble).  Elsewhere aR is within 2.5e-5 of 0 or 1 and the
+                // as W (rr + aR sm) + Delta, which is aR g + Delta in exact arithmetic, but the
+                // red populations of a source then sum to S rr + aR sum(W sm) (sm sums to zero)
+                // whatever the rounding of aR, where aR g emits S aR rho: in a near-steady state
+                // the quotient's rounding error repeats step after step and its sum over the
+                // interface moved the 64^3 D3Q19 bubble's red mass by 7e-6 in 10^4 steps
+                // (3.5e-7 with this form).  Elsewhere aR is within 2.5e-5 of 0 or 1 and the
                 // populations are aR g.
                 auto red_pop = [&](float rr_, float smv, float gv, float dl, int i, int j, bool withd) -> float {
                     if (!withd) return aR * gv;

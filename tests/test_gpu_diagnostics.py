@@ -35,9 +35,10 @@ def test_bubble_mass_conservation_10k_steps():
     (relative) over 10^4 steps.
 
     The red (bubble) phase is the 7 % of the mass, so its relative drift shows the colour split's
-    rounding most.  With red populations formed as aR g, the bias of the colour fraction's
-    rounding near rho = 1 drifted it by 7e-6; the kernel forms them as W (rr + aR sm) + Delta on
-    closed lattices, whose sum over a source's directions does not depend on that rounding.  The
+    rounding most.  With red populations formed as aR g, the colour fraction's rounding error
+    (repeating step after step in the near-steady bubble) drifted it by 7e-6; the kernel forms them
+    as W (rr + aR sm) + Delta on interface warps, whose sum over a source's directions does not
+    carry that rounding (tests/test_colour_split.py restates the arithmetic on the host).  The
     floor of FP32 storage itself, measured with FP64 arithmetic and the state rounded to FP32
     after every step (tests/test_mass_floor.py, opt-in), is 6.9e-7 for red and 8.6e-8 for blue."""
     p = mbcg.bubble_params(64, q=19, conservative=True)
