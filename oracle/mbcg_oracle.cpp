@@ -31,6 +31,7 @@
 #include <cstdint>
 #include <cstring>
 #include <algorithm>
+#include <vector>
 
 #include "../include/mbcg.h"
 
@@ -151,6 +152,12 @@ struct Oracle {
     int64_t sx, sy, sz; // dense strides
     R *const *A;
     R *const *B;
+    // Per-step caches of psi at every node and of the colour gradient F at every interface node
+    // of state A (filled by rcs before the node loop).  The reference recomputes F of a source
+    // for each direction that pulls from it; both caches hold the same numbers, computed by the
+    // same expressions in the same order, so the results are the same bits at a fraction of the
+    // cost on interface-heavy lattices.
+    mutable std::vector<R> psi_c, F_c;
 
     Oracle(const mbcg_params &pp, R *const *a, R *const *b) : p(pp), A(a), B(b) {
         k.build(p);
@@ -245,7 +252,7 @@ struct Oracle {
             v[1] = force_coord(1, n[1] + CY[i]);
             v[2] = force_coord(2, n[2] + CZ[i]);
             const int64_t idn = id3(v);
-            const R psi_n = psi(A[0][idn], A[1][idn]);
+            const R psi_n = psi_c.empty() ? psi(A[0][idn], A[1][idn]) : psi_c[idn];
             sx_ += k.w[i] * psi_n * k.c[0][i];
             sy_ += k.w[i] * psi_n * k.c[1][i];
             sz_ += k.w[i] * psi_n * k.c[2][i];
@@ -312,7 +319,13 @@ struct Oracle {
         R Deltai = 0;
         if (interface_indicator > static_cast<R>(1.0e-4)) {
             R Fx, Fy, Fz;
-            force(n, Fx, Fy, Fz);
+            if (F_c.empty()) {
+                force(n, Fx, Fy, Fz);
+            } else {
+                Fx = F_c[3 * src];
+                Fy = F_c[3 * src + 1];
+                Fz = F_c[3 * src + 2];
+            }
             const R Acoef = k.sigma_over_4cs4 / (k.tau_var ? tau_eff(rhor_s, rhob_s) : k.taub);
             const R absF = my_sqrt(Fx * Fx + Fy * Fy + Fz * Fz);
             if (!p.omega2_conservative || absF > static_cast<R>(1.0e-4)) gi += omega2(i, Fx, Fy, Fz, absF, Acoef);
@@ -434,8 +447,29 @@ struct Oracle {
         B[10][o] = Pxz;
     }
 
+    // the interface test of bulk() (lbm.cuh:181,187) at node o of state A
+    bool interface_node(int64_t o) const {
+        const R rhor_s = A[0][o], rhob_s = A[1][o];
+        const R inv_rhos = static_cast<R>(1) / (rhor_s + rhob_s);
+        return static_cast<R>(4) * rhor_s * rhob_s * inv_rhos * inv_rhos > static_cast<R>(1.0e-4);
+    }
+
     void rcs(int threads) const {
         const int z0 = 1, z1 = N[2] - 1;
+        const int64_t n_all = int64_t(N[0]) * N[1] * N[2];
+        psi_c.assign(n_all, static_cast<R>(0));
+        F_c.assign(3 * n_all, static_cast<R>(0));
+#pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
+        for (int64_t o = 0; o < n_all; ++o) psi_c[o] = psi(A[0][o], A[1][o]);
+#pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
+        for (int z = 0; z < N[2]; ++z)
+            for (int y = 0; y < N[1]; ++y)
+                for (int x = 0; x < N[0]; ++x) {
+                    const int64_t o = id(x, y, z);
+                    if (!interface_node(o)) continue;
+                    const int n[3] = {x, y, z};
+                    force(n, F_c[3 * o], F_c[3 * o + 1], F_c[3 * o + 2]);
+                }
 #pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
         for (int z = z0; z < z1; ++z)
             for (int y = 1; y < N[1] - 1; ++y)
