@@ -213,10 +213,11 @@ def cpu_leg(budget_s: float, threads: int, real_bytes: int = 4) -> dict:
     dtype = np.float32 if real_bytes == 4 else np.float64
     a = ol.oracle_init(p, dtype)
     b = a.copy()
-    ol.oracle_step(p, a, 1, threads=threads, b=b)  # warm
+    # the reference's cost structure: each source's colour gradient recomputed per direction
+    ol.oracle_step(p, a, 1, threads=threads, b=b, reference_cost=True)  # warm
     steps, t0 = 0, time.perf_counter()
     while True:
-        ol.oracle_step(p, a, steps + 2, threads=threads, b=b)
+        ol.oracle_step(p, a, steps + 2, threads=threads, b=b, reference_cost=True)
         a, b = b, a
         steps += 1
         dt = time.perf_counter() - t0

@@ -157,7 +157,15 @@ struct Oracle {
     // for each direction that pulls from it; both caches hold the same numbers, computed by the
     // same expressions in the same order, so the results are the same bits at a fraction of the
     // cost on interface-heavy lattices.
-    mutable std::vector<R> psi_c, F_c;
+    // The storage lives per calling thread across steps (no allocation per step); only the
+    // entries rcs fills are read.
+    static std::vector<R> &cache_store(int which) {
+        thread_local std::vector<R> store[2];
+        return store[which];
+    }
+    std::vector<R> &psi_c = cache_store(0);
+    std::vector<R> &F_c = cache_store(1);
+    mutable bool psi_ready = false, F_ready = false;
 
     Oracle(const mbcg_params &pp, R *const *a, R *const *b) : p(pp), A(a), B(b) {
         k.build(p);
@@ -252,7 +260,7 @@ struct Oracle {
             v[1] = force_coord(1, n[1] + CY[i]);
             v[2] = force_coord(2, n[2] + CZ[i]);
             const int64_t idn = id3(v);
-            const R psi_n = psi_c.empty() ? psi(A[0][idn], A[1][idn]) : psi_c[idn];
+            const R psi_n = psi_ready ? psi_c[idn] : psi(A[0][idn], A[1][idn]);
             sx_ += k.w[i] * psi_n * k.c[0][i];
             sy_ += k.w[i] * psi_n * k.c[1][i];
             sz_ += k.w[i] * psi_n * k.c[2][i];
@@ -319,7 +327,7 @@ struct Oracle {
         R Deltai = 0;
         if (interface_indicator > static_cast<R>(1.0e-4)) {
             R Fx, Fy, Fz;
-            if (F_c.empty()) {
+            if (!F_ready) {
                 force(n, Fx, Fy, Fz);
             } else {
                 Fx = F_c[3 * src];
@@ -454,22 +462,29 @@ struct Oracle {
         return static_cast<R>(4) * rhor_s * rhob_s * inv_rhos * inv_rhos > static_cast<R>(1.0e-4);
     }
 
-    void rcs(int threads) const {
+    // cached: the colour gradient once per interface node (the default); otherwise once per
+    // (destination, direction) as the reference computes it (the timed CPU baseline)
+    void rcs(int threads, bool cached) const {
         const int z0 = 1, z1 = N[2] - 1;
-        const int64_t n_all = int64_t(N[0]) * N[1] * N[2];
-        psi_c.assign(n_all, static_cast<R>(0));
-        F_c.assign(3 * n_all, static_cast<R>(0));
+        psi_ready = F_ready = false;
+        if (cached) {
+            const int64_t n_all = int64_t(N[0]) * N[1] * N[2];
+            if (static_cast<int64_t>(psi_c.size()) < n_all) psi_c.resize(n_all);
+            if (static_cast<int64_t>(F_c.size()) < 3 * n_all) F_c.resize(3 * n_all);
 #pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
-        for (int64_t o = 0; o < n_all; ++o) psi_c[o] = psi(A[0][o], A[1][o]);
+            for (int64_t o = 0; o < n_all; ++o) psi_c[o] = psi(A[0][o], A[1][o]);
+            psi_ready = true;
 #pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
-        for (int z = 0; z < N[2]; ++z)
-            for (int y = 0; y < N[1]; ++y)
-                for (int x = 0; x < N[0]; ++x) {
-                    const int64_t o = id(x, y, z);
-                    if (!interface_node(o)) continue;
-                    const int n[3] = {x, y, z};
-                    force(n, F_c[3 * o], F_c[3 * o + 1], F_c[3 * o + 2]);
-                }
+            for (int z = 0; z < N[2]; ++z)
+                for (int y = 0; y < N[1]; ++y)
+                    for (int x = 0; x < N[0]; ++x) {
+                        const int64_t o = id(x, y, z);
+                        if (!interface_node(o)) continue;
+                        const int n[3] = {x, y, z};
+                        force(n, F_c[3 * o], F_c[3 * o + 1], F_c[3 * o + 2]);
+                    }
+            F_ready = true;
+        }
 #pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
         for (int z = z0; z < z1; ++z)
             for (int y = 1; y < N[1] - 1; ++y)
@@ -705,7 +720,7 @@ int step_impl(const mbcg_params *p, void *const *a, void *const *b, int64_t step
         B[f] = static_cast<R *>(b[f]);
     }
     Oracle<R> o(*p, A, B);
-    if (do_rcs) o.rcs(threads);
+    if (do_rcs) o.rcs(threads, do_rcs != 2);
     if (do_bc) o.bc(B, A, step);
     return 0;
 }
@@ -724,7 +739,8 @@ int init_impl(const mbcg_params *p, void *const *a) {
 extern "C" {
 
 // One time step on dense (pitch = nx) host arrays of 4-byte (float) or 8-byte (double)
-// reals: RCS A -> B over the fluid nodes (if do_rcs), then the inlet/outlet functors on B
+// reals: RCS A -> B over the fluid nodes (if do_rcs; 2: with the colour gradient recomputed for
+// every direction as the reference does, same results), then the inlet/outlet functors on B
 // reading the old state A (if do_bc).  step = index of the state B holds.
 int oracle_step(const mbcg_params *p, int real_bytes, void *const *a, void *const *b, int64_t step, int do_rcs,
                 int do_bc, int threads) {

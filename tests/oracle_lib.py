@@ -69,13 +69,16 @@ def oracle_init(p: mbcg.Params, dtype=np.float64) -> np.ndarray:
 
 
 def oracle_step(p: mbcg.Params, a: np.ndarray, step: int, do_rcs=True, do_bc=True, threads=None,
-                b: np.ndarray = None) -> np.ndarray:
+                b: np.ndarray = None, reference_cost: bool = False) -> np.ndarray:
     """One step A -> B (B starts as a copy of A so ghost layers carry over, as the
-    reference's ping-pong buffers do after the first steps)."""
+    reference's ping-pong buffers do after the first steps).  reference_cost: recompute each
+    source's colour gradient for every direction, as the reference does (same results; the
+    timed CPU baseline), instead of once per node."""
     if b is None:
         b = a.copy()
     threads = threads or os.cpu_count() or 1
-    rc = oracle().oracle_step(ctypes.byref(p), a.itemsize, _ptrs(a), _ptrs(b), int(step), int(do_rcs),
+    rcs = (2 if reference_cost else 1) if do_rcs else 0
+    rc = oracle().oracle_step(ctypes.byref(p), a.itemsize, _ptrs(a), _ptrs(b), int(step), rcs,
                               int(do_bc), int(threads))
     assert rc == 0
     return b

@@ -56,6 +56,18 @@ def test_random_state_fp32_bitexact(q):
     a = z["in_float"]
     np.testing.assert_array_equal(ol.oracle_step(p, a, 1, do_bc=False), z["rcs_float"])
     np.testing.assert_array_equal(ol.oracle_step(p, a, 1), z["out_float"])
+    # the reference's cost structure (colour gradient recomputed per direction, the timed CPU
+    # baseline) gives the same bits as the per-node gradient cache
+    np.testing.assert_array_equal(ol.oracle_step(p, a, 1, reference_cost=True), z["out_float"])
+
+
+@pytest.mark.parametrize("real", [np.float32, np.float64])
+def test_gradient_cache_is_bit_identical(real):
+    """Interface-heavy cases with walls, force and a density ratio: one step with the per-node
+    colour-gradient cache equals one step with the reference's per-direction recomputation."""
+    for p in (mbcg.rti_params(16, q=27), mbcg.bubble_params(16, q=19, radius=4.0)):
+        a = ol.oracle_run(p, ol.oracle_init(p, real), 3)
+        np.testing.assert_array_equal(ol.oracle_step(p, a, 4), ol.oracle_step(p, a, 4, reference_cost=True))
 
 
 @pytest.mark.parametrize("q", [27, 19])
