@@ -63,3 +63,14 @@ def test_operators_compile_for_the_gpu(tmp_path):
         pytest.skip("nvcc not available")
     subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "--expt-relaxed-constexpr",
                     f"-I{os.path.join(ROOT, 'include')}", "-c", src, "-o", src + ".o"], check=True)
+
+
+def test_operator_invariants(tmp_path):
+    """tests/cpp/invariants.cpp, in FP64 for D3Q27 and D3Q19: the weights sum to 1 and B to 1/3;
+    sum_i w_i cos2rule_i = cs^2 (cos2rule omits 1/|c_i|^2); Omega2 has zero sum and zero first
+    moment above |F| = 1e-4; the recolouring terms cancel over c_i and -c_i."""
+    exe = os.path.join(str(tmp_path), "invariants")
+    subprocess.run(["g++", "-std=c++20", "-O2", f"-I{os.path.join(ROOT, 'include')}",
+                    os.path.join(ROOT, "tests", "cpp", "invariants.cpp"), "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout
